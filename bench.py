@@ -1,0 +1,354 @@
+"""Benchmark of the restarted-PDHG solve loop (KKT matrix passes per second).
+
+Workload (default): the transportation LP — 500 supply x 2,000 demand nodes, 1,000,000
+variables, 2,500 constraints, 2,000,000 nonzeros, FP64, relative KKT tolerance 1e-4,
+seeded synthetic data. One step = one full solve from the zero start to termination
+under the reference's own criteria, with the scaled problem already resident in HBM.
+
+  value       KKT matrix passes / s (the reference's cumulative_kkt_matrix_passes per
+              second of solve time), timed with CUDA events on the solver's stream.
+  e2e         the same metric through the C ABI with host buffers: gpdhg_problem_create
+              (host->device copy of the CSR matrix and vectors, transpose and schedule),
+              gpdhg_solve, and the device->host copy of the solution, every step.
+  roofline    the dominant step kernel's algorithmic bytes / its CUDA-event time, measured
+              live over the timed steps (params.profile_kernels).
+  cpu_baseline  the oracle (the CPU FP64 restatement of the reference loop) on the host
+              cores over a bounded sample of the same workload.
+
+--impl reference times that CPU implementation alone (the reference itself is Julia
+and cannot be installed here). Multi-GPU: replicas only (a single LP does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "cupdlp.jl_gb300"))
+
+import numpy as np  # noqa: E402
+
+L2_BYTES = 129 * 2**20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="transportation", choices=["transportation", "plain", "powerlaw"])
+    ap.add_argument("--tolerance", type=float, default=1e-4)
+    ap.add_argument("--cpu-sample-iters", type=int, default=0, help="oracle iteration cap (0: automatic)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(name):
+    import cupdlp
+    from cupdlp import synthetic
+    if name == "transportation":
+        lp = synthetic.transportation_lp(1)
+        prec = cupdlp.Precision.FP64
+        desc = "transportation LP 500x2000: m=2,500, n=1,000,000, nnz=2,000,000, FP64"
+    elif name == "plain":
+        lp = synthetic.known_optimum_lp(0)
+        prec = cupdlp.Precision.FP64
+        desc = "plain LP with planted optimum: m=1,000, n=2,000, nnz=10,000, FP64"
+    else:
+        lp = synthetic.power_law_lp(2)
+        prec = cupdlp.Precision.FP32_REFINE
+        desc = "power-law LP: m=1,000,000, n=2,000,000, nnz~20M, FP32 bulk + FP64 refinement"
+    return lp, prec, desc
+
+
+def bytes_model(m, n, nnz, prec):
+    """Algorithmic bytes of the two step kernels (minimum traffic of the fused schedule,
+    gathered vectors counted once)."""
+    sv = 8 if prec == 0 else 4   # matrix values
+    sx = sv                      # iterate vectors
+    si = 4                       # int32 indices
+    mat_t = (sv + si) * nnz + si * (n + 1)   # CSR of A' (n rows)
+    mat_a = (sv + si) * nnz + si * (m + 1)   # CSR of A (m rows)
+    return {
+        # primal kernel with a commit: A' stream, gather y, read x dx c l u sx skty,
+        # write x dx kty sx skty
+        "primal_commit": mat_t + sx * m + 12 * sx * n,
+        # primal kernel after a rejection: read x kty c l u, write dx
+        "primal_plain": 6 * sx * n,
+        # dual kernel: A stream, gather dx, read y kx b, write y' kx'
+        "dual": mat_a + sx * n + 5 * sx * m,
+        # extra dual traffic when it commits the sums: sy skx read+write
+        "dual_commit_extra": 4 * sx * m,
+    }
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        rows = [r.split(", ") for r in open(self.path).read().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = max(float(r[2]) for r in rows)
+        load = [v for v in sm if v > 0.5 * mx] or sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip() == "Active"})
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl"
+        try:
+            import torch
+            torch.cuda.set_device(local)
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_baseline(lp_problem, params, iters_cap, threads=None):
+    """The oracle on a bounded sample: the first `iters_cap` iterations of the same solve."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    import cupdlp
+    threads = threads or os.cpu_count() or 1
+    oracle.set_threads(threads)
+    sq = cupdlp.rescale_problem(10, False, 1.0, 0, lp_problem)
+    p = cupdlp.default_parameters(tolerance=params.termination_criteria.eps_optimal_relative,
+                                  iteration_limit=iters_cap)
+    t0 = time.perf_counter()
+    run = oracle.solve_scaled(sq, p, max_stats=100)
+    wall = time.perf_counter() - t0
+    r = run.result
+    return {"value": r.cumulative_kkt_matrix_passes / r.solve_time_sec, "unit": "KKT passes/s", "cores": threads,
+            "kind": "port",
+            "sample": f"oracle FP64 restatement, first {r.iteration_count} iterations "
+                      f"({r.cumulative_kkt_matrix_passes:.0f} KKT passes, {r.solve_time_sec:.1f} s of loop, "
+                      f"{wall:.1f} s wall)"}
+
+
+def run_reference(args):
+    world, rank, local, pg = dist_setup(args.gpus)
+    if rank != 0:
+        return 0
+    import cupdlp
+    lp, prec, desc = workload(args.workload)
+    params = cupdlp.default_parameters(tolerance=args.tolerance, precision=prec)
+    cap = args.cpu_sample_iters or {"transportation": 400, "plain": 3000, "powerlaw": 40}[args.workload]
+    vals = []
+    for k in range(args.warmup + args.steps):
+        cb = cpu_baseline(lp.problem, params, cap)
+        if k >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.mean(vals))
+    line = {"metric": "KKT mults/sec", "value": v, "unit": "KKT passes/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": desc, "tolerance": args.tolerance, "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": v, "unit": "KKT passes/s", "cores": cb["cores"], "kind": "port",
+                             "sample": cb["sample"]},
+            "e2e": {"value": v, "unit": "KKT passes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    world, rank, local, pg = dist_setup(args.gpus)
+    import torch
+    import cupdlp
+    from cupdlp.solver import DeviceProblem, scaled_desc
+    torch.cuda.set_device(local)
+    torch.zeros(1, device="cuda")
+    lp, prec, desc = workload(args.workload)
+    params = cupdlp.default_parameters(tolerance=args.tolerance, precision=prec, record_iteration_stats=False)
+    sq = cupdlp.rescale_problem(10, False, 1.0, 0, lp.problem)
+    d = scaled_desc(sq)
+    m, n, nnz = d.desc.num_constraints, d.desc.num_variables, d.desc.nnz
+    dp = DeviceProblem(d)
+    stream = torch.cuda.ExternalStream(dp.lib.gpdhg_problem_stream(dp.handle))
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        dp.solve(params, want_solution=False)
+
+    params.profile_kernels = True
+    cparams = cupdlp.params_to_c(params)
+    cparams.profile_kernels = 1
+    import ctypes as C
+    from cupdlp import _abi
+    results = []
+    ms_total = 0.0
+    barrier(pg)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            res = _abi.Result()
+            _abi.check(dp.lib.gpdhg_solve(dp.handle, C.byref(cparams), C.byref(res), None, None), dp.lib)
+            e1.record(stream)
+            e1.synchronize()
+            ms_total += e0.elapsed_time(e1)
+            results.append(res)
+    torch.cuda.synchronize()
+    barrier(pg)
+    clocks = clk.summary()
+    kkt = sum(r.cumulative_kkt_matrix_passes for r in results)
+    t_max = max_over_ranks(pg, ms_total / 1e3)
+    kkt_all = sum_over_ranks(pg, kkt)
+    value = kkt_all / t_max
+    launches = sum(r.kernels_launched for r in results)
+
+    # roofline of the dominant step kernel, from the live per-kernel CUDA events
+    bm = bytes_model(m, n, nnz, 0 if prec == cupdlp.Precision.FP64 else 1)
+    attempts = sum(r.primal_kernel_launches for r in results)
+    spmv = sum(r.primal_spmv_launches for r in results)
+    tp = sum(r.primal_kernel_sec for r in results)
+    td = sum(r.dual_kernel_sec for r in results)
+    bytes_p = spmv * bm["primal_commit"] + (attempts - spmv) * bm["primal_plain"]
+    bytes_d = attempts * bm["dual"] + spmv * bm["dual_commit_extra"]
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    dom = "primal_step_kernel" if tp >= td else "dual_step_kernel"
+    b_dom, t_dom = (bytes_p, tp) if tp >= td else (bytes_d, td)
+    achieved = (b_dom / t_dom / 1e9) if t_dom > 0 else None
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
+                "share_of_step_time": {"primal_step_kernel": tp / max(tp + td, 1e-30),
+                                       "dual_step_kernel": td / max(tp + td, 1e-30)},
+                "bytes_per_launch": {"primal_with_commit": bm["primal_commit"], "dual": bm["dual"]},
+                "step_pair_GBps": ((bytes_p + bytes_d) / (tp + td) / 1e9) if tp + td > 0 else None}
+
+    # e2e through the C ABI with host buffers (create -> solve -> copy back), every step
+    e2e_times, e2e_kkt = [], 0.0
+    h2d = sum(a.nbytes for a in d.arrays.values() if a is not None)
+    d2h = 8 * (n + m)
+    for k in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        with DeviceProblem(d) as dq:
+            r, x, y = dq.solve(params, want_solution=True)
+        e2e_times.append(time.perf_counter() - t0)
+        e2e_kkt += r.cumulative_kkt_matrix_passes
+    e2e_value = e2e_kkt / sum(e2e_times)
+
+    cb = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cap = args.cpu_sample_iters or {"transportation": 400, "plain": 3000, "powerlaw": 40}[args.workload]
+        cb = cpu_baseline(lp.problem, params, cap)
+
+    r0 = results[-1]
+    ci = r0.last_iteration_stats.convergence_information
+    line = {
+        "metric": "KKT mults/sec", "value": value, "unit": "KKT passes/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == cupdlp.Precision.FP64 else "f32+f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": desc, "tolerance": args.tolerance, "parallelism": f"replicas x{world}",
+                   "l2": "flushed between steps (256 MB write); working set > L2",
+                   "iterations_per_solve": r0.iteration_count, "attempts_per_solve": r0.total_number_iterations,
+                   "kkt_passes_per_solve": r0.cumulative_kkt_matrix_passes,
+                   "termination": int(r0.termination_reason), "primal_objective": ci.primal_objective,
+                   "dual_objective": ci.dual_objective},
+        "e2e": {"value": e2e_value, "unit": "KKT passes/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "sec_per_step": statistics.mean(e2e_times)},
+        "roofline": roofline,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    if cb:
+        line["cpu_baseline"] = cb
+    dp.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

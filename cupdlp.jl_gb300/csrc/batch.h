@@ -1,0 +1,50 @@
+// batch.h — the packed multi-LP layout behind gpdhg_batch.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "host_logic.h"
+#include "problem.h"
+
+namespace gpdhg {
+
+constexpr int kSegLen = 4096;   // elements per segmented-reduction item
+
+template <class T>
+struct BatchWorkspace;
+struct BatchWorkspaceDeleter {
+  void operator()(BatchWorkspace<double>* w) const;
+  void operator()(BatchWorkspace<float>* w) const;
+};
+
+// Splits [off[k], off[k+1]) of every instance into kSegLen-element items.
+void build_seg_items(const std::vector<int32_t>& off, std::vector<SegItem>& items, std::vector<int32_t>& begin);
+
+}  // namespace gpdhg
+
+struct gpdhg_batch {
+  int32_t count = 0;
+  int32_t M = 0, N = 0;                        // packed rows / columns
+  std::vector<int32_t> row_off, col_off, neq;  // per instance (offsets: count + 1)
+  std::vector<gpdhg::InstanceInfo> info;
+  std::vector<double> amax, norm_b, norm_c;
+  gpdhg::DeviceMatrix A, At;                   // block-diagonal CSR of A and A'
+  gpdhg::DBuf<int32_t> item_inst_p, item_inst_d, p_item_begin, d_item_begin, row_off_d, neq_d;
+  gpdhg::DBuf<double> l, u, c, b, ol, ou, oc, ob, con, var;
+  gpdhg::DBuf<uint8_t> ineq_flag;              // per packed row: a '>=' row
+  gpdhg::DBuf<int32_t> col_inst, row_inst;     // instance of each packed column / row
+  gpdhg::DBuf<gpdhg::SegItem> seg_n, seg_m;
+  gpdhg::DBuf<int32_t> seg_n_begin, seg_m_begin;
+  int nseg_n = 0, nseg_m = 0;
+  cudaStream_t stream = nullptr;
+  std::unique_ptr<gpdhg::BatchWorkspace<double>, gpdhg::BatchWorkspaceDeleter> ws64;
+  std::unique_ptr<gpdhg::BatchWorkspace<float>, gpdhg::BatchWorkspaceDeleter> ws32;
+  ~gpdhg_batch();
+};
+
+namespace gpdhg {
+void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs);
+void batch_solve(gpdhg_batch* B, const gpdhg_params& prm, gpdhg_result* results, double* const* primal_out,
+                 double* const* dual_out);
+}  // namespace gpdhg

@@ -1,0 +1,261 @@
+// eval_kernels.cuh — FP64 reductions for termination checks and restart scoring.
+//
+// The reference computes each statistic with its own broadcast kernel and a host
+// round trip per norm, and allocates temporaries for concatenated norms
+// (src/iteration_stats_utils_gpu.jl:23-372, src/saddle_point_gpu.jl:250-278). Here every
+// statistic of one evaluation is accumulated in FP64 in a single grid-stride pass per
+// side (n columns, m rows), into per-CTA partials that one finalize CTA reduces in a
+// fixed order; the host reads back one small array.
+#pragma once
+
+#include "common.cuh"
+
+namespace gpdhg {
+
+__device__ __forceinline__ double nan_max(double a, double b) { return (a != a || b != b) ? a + b : fmax(a, b); }
+
+__device__ __forceinline__ double warp_nan_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = nan_max(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__device__ __forceinline__ double block_nan_max(double v, double* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_nan_max(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    r = warp_nan_max(r);
+  }
+  return r;
+}
+
+// Grid-stride reduction of Q quantities; bit q of MAXMASK selects max (else sum).
+// All max-quantities are magnitudes, so 0 is their identity.
+template <int Q, unsigned MAXMASK, class F>
+__global__ void __launch_bounds__(kBlock) reduce_kernel(long long len, F f, double* partials) {
+  __shared__ double sh[32];
+  double acc[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) acc[q] = 0.0;
+  const long long stride = (long long)gridDim.x * kBlock;
+  for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < len; i += stride) f(i, acc);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const double r = ((MAXMASK >> q) & 1u) ? block_nan_max(acc[q], sh) : block_sum(acc[q], sh);
+    if (threadIdx.x == 0) partials[q * gridDim.x + blockIdx.x] = r;
+  }
+}
+
+template <int Q, unsigned MAXMASK>
+__global__ void __launch_bounds__(kBlock) finalize_kernel(const double* partials, int nb, double* out) {
+  __shared__ double sh[32];
+  for (int q = 0; q < Q; ++q) {
+    const bool is_max = (MAXMASK >> q) & 1u;
+    double a = 0.0;
+    for (int k = threadIdx.x; k < nb; k += kBlock) {
+      const double v = partials[q * nb + k];
+      a = is_max ? nan_max(a, v) : a + v;
+    }
+    a = is_max ? block_nan_max(a, sh) : block_sum(a, sh);
+    if (threadIdx.x == 0) out[q] = a;
+  }
+}
+
+__device__ __forceinline__ double reduced_cost(double g, bool fl, bool fu) {
+  // src/iteration_stats_utils_gpu.jl:168: max(g,0)*isfinite(l) + min(g,0)*isfinite(u)
+  return (fl ? jmax(g, 0.0) : 0.0) + (fu ? jmin(g, 0.0) : 0.0);
+}
+__device__ __forceinline__ double rc_contribution(double rc, double l, double u) {
+  // src/iteration_stats_utils_gpu.jl:120-126
+  return rc > 0.0 ? l * rc : (rc < 0.0 ? u * rc : 0.0);
+}
+
+// Unscaled primal-side statistics of the averaged iterate (original problem).
+enum EvalNQ {
+  kN_LuSq = 0, kN_LuMax, kN_Cx, kN_XMax, kN_XSq, kN_RcvSq, kN_RcvMax, kN_Contrib,
+  kN_RayLuMax, kN_RayRcvMax, kN_RayContrib, kN_RayRcMax, kEvalNQ
+};
+constexpr unsigned kEvalNMax = (1u << kN_LuMax) | (1u << kN_XMax) | (1u << kN_RcvMax) | (1u << kN_RayLuMax) |
+                               (1u << kN_RayRcvMax) | (1u << kN_RayRcMax);
+
+template <class T>
+struct EvalN {
+  const T* ax;
+  const T* agrad;
+  const double* var;   // variable_rescaling (D)
+  const double* ol;
+  const double* ou;
+  const double* oc;
+  __device__ __forceinline__ void operator()(long long j, double* a) const {
+    const double x = (double)ax[j] / var[j];       // :470-471
+    const double g = (double)agrad[j] * var[j];    // :472-473
+    const double l = ol[j], u = ou[j], c = oc[j];
+    const bool fl = isfinite(l), fu = isfinite(u);
+    const double lv = jmax(l - x, 0.0), uv = jmax(x - u, 0.0);
+    a[kN_LuSq] += lv * lv + uv * uv;
+    a[kN_LuMax] = nan_max(a[kN_LuMax], nan_max(fabs(lv), fabs(uv)));
+    a[kN_Cx] += c * x;
+    a[kN_XMax] = nan_max(a[kN_XMax], fabs(x));
+    a[kN_XSq] += x * x;
+    const double rc = reduced_cost(g, fl, fu);
+    const double rcv = g - rc;
+    a[kN_RcvSq] += rcv * rcv;
+    a[kN_RcvMax] = nan_max(a[kN_RcvMax], fabs(rcv));
+    a[kN_Contrib] += rc_contribution(rc, l, u);
+    // primal ray, before division by ||x||_inf: bounds 0 where finite (:335-336)
+    const double lr = fl ? jmax(-x, 0.0) : 0.0, ur = fu ? jmax(x, 0.0) : 0.0;
+    a[kN_RayLuMax] = nan_max(a[kN_RayLuMax], nan_max(lr, ur));
+    // dual ray: objective set to zero, gradient - c (:346-354)
+    const double gr = g - c;
+    const double rcr = reduced_cost(gr, fl, fu);
+    a[kN_RayRcvMax] = nan_max(a[kN_RayRcvMax], fabs(gr - rcr));
+    a[kN_RayContrib] += rc_contribution(rcr, l, u);
+    a[kN_RayRcMax] = nan_max(a[kN_RayRcMax], fabs(rcr));
+  }
+};
+
+enum EvalMQ { kM_CvSq = 0, kM_CvMax, kM_DrSq, kM_DrMax, kM_By, kM_YMax, kM_YSq, kM_RayCvMax, kEvalMQ };
+constexpr unsigned kEvalMMax = (1u << kM_CvMax) | (1u << kM_DrMax) | (1u << kM_YMax) | (1u << kM_RayCvMax);
+
+template <class T>
+struct EvalM {
+  const T* ay;
+  const T* akx;
+  const double* con;   // constraint_rescaling (E)
+  const double* ob;
+  int neq;
+  const uint8_t* ineq_flag;  // per-row '>=' flag (packed batches); NULL: rows >= neq
+  __device__ __forceinline__ void operator()(long long i, double* a) const {
+    const double y = (double)ay[i] / con[i];       // :474-475
+    const double kx = (double)akx[i] * con[i];     // :476-477
+    const double b = ob[i];
+    const bool ineq = ineq_flag ? ineq_flag[i] != 0 : i >= neq;
+    double cv = b - kx;                            // :26-45
+    if (ineq) cv = jmax(cv, 0.0);
+    a[kM_CvSq] += cv * cv;
+    a[kM_CvMax] = nan_max(a[kM_CvMax], fabs(cv));
+    if (ineq) {
+      const double dr = jmax(-y, 0.0);             // :198-211
+      a[kM_DrSq] += dr * dr;
+      a[kM_DrMax] = nan_max(a[kM_DrMax], dr);
+    }
+    a[kM_By] += b * y;
+    a[kM_YMax] = nan_max(a[kM_YMax], fabs(y));
+    a[kM_YSq] += y * y;
+    double cvr = -kx;                              // ray: right-hand side 0 (:338)
+    if (ineq) cvr = jmax(cvr, 0.0);
+    a[kM_RayCvMax] = nan_max(a[kM_RayCvMax], fabs(cvr));
+  }
+};
+
+// Scaled weighted-KKT ingredients (src/saddle_point_gpu.jl:250-278) of three points:
+// 0 = current, 1 = average, 2 = last restart; plus ||avg - last restart||^2.
+constexpr int kKktNQ = 13;
+constexpr int kKktMQ = 10;
+
+template <class T>
+struct KktN {
+  const T* l;
+  const T* u;
+  const T* c;
+  const T* x0; const T* x1; const T* x2;
+  const T* g0; const T* g1; const T* g2;
+  __device__ __forceinline__ void point(int p, const T* xs, const T* gs, long long j, double l, double u, double c,
+                                        bool fl, bool fu, double* a) const {
+    const double x = (double)xs[j], g = (double)gs[j];
+    const double lv = jmax(l - x, 0.0), uv = jmax(x - u, 0.0);
+    a[4 * p + 0] += lv * lv + uv * uv;
+    a[4 * p + 1] += c * x;
+    const double rc = reduced_cost(g, fl, fu);
+    const double rcv = g - rc;
+    a[4 * p + 2] += rcv * rcv;
+    a[4 * p + 3] += rc_contribution(rc, l, u);
+  }
+  __device__ __forceinline__ void operator()(long long j, double* a) const {
+    const double l = (double)this->l[j], u = (double)this->u[j], c = (double)this->c[j];
+    const bool fl = isfinite(l), fu = isfinite(u);
+    point(0, x0, g0, j, l, u, c, fl, fu, a);
+    point(1, x1, g1, j, l, u, c, fl, fu, a);
+    point(2, x2, g2, j, l, u, c, fl, fu, a);
+    const double d = (double)x1[j] - (double)x2[j];
+    a[12] += d * d;
+  }
+};
+
+template <class T>
+struct KktM {
+  const T* b;
+  const T* y0; const T* y1; const T* y2;
+  const T* k0; const T* k1; const T* k2;
+  int neq;
+  const uint8_t* ineq_flag;  // as in EvalM
+  __device__ __forceinline__ void point(int p, const T* ys, const T* ks, long long i, double b, bool ineq,
+                                        double* a) const {
+    const double y = (double)ys[i], kx = (double)ks[i];
+    double cv = b - kx;
+    if (ineq) cv = jmax(cv, 0.0);
+    a[3 * p + 0] += cv * cv;
+    if (ineq) {
+      const double dr = jmax(-y, 0.0);
+      a[3 * p + 1] += dr * dr;
+    }
+    a[3 * p + 2] += b * y;
+  }
+  __device__ __forceinline__ void operator()(long long i, double* a) const {
+    const double b = (double)this->b[i];
+    const bool ineq = ineq_flag ? ineq_flag[i] != 0 : i >= neq;
+    point(0, y0, k0, i, b, ineq, a);
+    point(1, y1, k1, i, b, ineq, a);
+    point(2, y2, k2, i, b, ineq, a);
+    const double d = (double)y1[i] - (double)y2[i];
+    a[9] += d * d;
+  }
+};
+
+// ---- small vector kernels --------------------------------------------------------
+
+template <class T>
+__global__ void grad_kernel(int n, const T* c, const T* kty, T* grad) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) grad[j] = c[j] - kty[j];
+}
+
+// compute_average!, src/saddle_point_gpu.jl:226-240
+template <class T>
+__global__ void average_n_kernel(int n, const T* sx, const T* skty, const T* c, double wx, double wy, T* ax,
+                                 T* agrad) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    ax[j] = (T)((double)sx[j] / wx);
+    const T g = (T)(-(double)skty[j] / wy);
+    agrad[j] = g + c[j];
+  }
+}
+template <class T>
+__global__ void average_m_kernel(int m, const T* sy, const T* skx, double wx, double wy, T* ay, T* akx) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    ay[i] = (T)((double)sy[i] / wy);
+    akx[i] = (T)((double)skx[i] / wx);
+  }
+}
+
+// restart to average, src/saddle_point_gpu.jl:579-583
+template <class T>
+__global__ void restart_n_kernel(int n, const T* ax, const T* agrad, const T* c, T* x, T* kty, T* grad) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    x[j] = ax[j];
+    kty[j] = c[j] - agrad[j];
+    grad[j] = agrad[j];
+  }
+}
+
+template <class S, class D>
+__global__ void convert_kernel(long long len, const S* src, D* dst) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = (D)src[i];
+}
+
+}  // namespace gpdhg

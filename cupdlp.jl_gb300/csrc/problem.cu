@@ -1,0 +1,191 @@
+// problem.cu — validation and upload of one LP (replaces src/cpu_to_gpu.jl:26-81).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "problem.h"
+
+namespace gpdhg {
+
+std::vector<RowItem> build_row_items(const int32_t* rp, int32_t nrows) {
+  std::vector<RowItem> items;
+  int32_t r = 0;
+  while (r < nrows) {
+    const int32_t start = r;
+    const int64_t base = rp[r];
+    if ((int64_t)rp[r + 1] - base > kItemNnz) {
+      items.push_back({r, r + 1});
+      ++r;
+      continue;
+    }
+    while (r < nrows && r - start < kRowsPerItem && (int64_t)rp[r + 1] - base <= kItemNnz) ++r;
+    items.push_back({start, r});
+  }
+  return items;
+}
+
+void transpose_csr(int32_t m, int32_t n, const int32_t* rp, const int32_t* col, const double* val, HostCsr& t) {
+  const int64_t nnz = rp[m];
+  t.row_ptr.assign((size_t)n + 1, 0);
+  t.col.resize(nnz);
+  t.val.resize(nnz);
+  for (int64_t k = 0; k < nnz; ++k) t.row_ptr[(size_t)col[k] + 1]++;
+  for (int32_t j = 0; j < n; ++j) t.row_ptr[j + 1] += t.row_ptr[j];
+  std::vector<int32_t> fill(t.row_ptr.begin(), t.row_ptr.end() - 1);
+  for (int32_t i = 0; i < m; ++i)
+    for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
+      const int32_t p = fill[col[k]]++;
+      t.col[p] = i;
+      t.val[p] = val[k];
+    }
+}
+
+namespace {
+
+void upload_matrix(DeviceMatrix& dm, int32_t nrows, int32_t ncols, const int32_t* rp, const int32_t* col,
+                   const double* val, cudaStream_t s) {
+  dm.nrows = nrows;
+  dm.ncols = ncols;
+  dm.nnz = rp[nrows];
+  dm.row_ptr.alloc((size_t)nrows + 1);
+  dm.col.alloc(std::max<long long>(dm.nnz, 1));
+  dm.val64.alloc(std::max<long long>(dm.nnz, 1));
+  CK(cudaMemcpyAsync(dm.row_ptr.get(), rp, sizeof(int32_t) * ((size_t)nrows + 1), cudaMemcpyHostToDevice, s));
+  if (dm.nnz) {
+    CK(cudaMemcpyAsync(dm.col.get(), col, sizeof(int32_t) * dm.nnz, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dm.val64.get(), val, sizeof(double) * dm.nnz, cudaMemcpyHostToDevice, s));
+  }
+  std::vector<RowItem> items = build_row_items(rp, nrows);
+  dm.num_items = (int32_t)items.size();
+  dm.items.alloc(std::max<size_t>(items.size(), 1));
+  if (!items.empty())
+    CK(cudaMemcpyAsync(dm.items.get(), items.data(), sizeof(RowItem) * items.size(), cudaMemcpyHostToDevice, s));
+  // the schedule vector dies at return: wait for the copies before it does
+  CK(cudaStreamSynchronize(s));
+}
+
+void upload_vec(DBuf<double>& d, const double* h, size_t n, cudaStream_t s) {
+  d.alloc(std::max<size_t>(n, 1));
+  if (n) CK(cudaMemcpyAsync(d.get(), h, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+}
+
+void upload_vec_or_fill(DBuf<double>& d, const double* h, const double* fallback, size_t n, cudaStream_t s) {
+  upload_vec(d, h ? h : fallback, n, s);
+}
+
+double norm2(const double* v, size_t n) {
+  double s = 0.0;
+  for (size_t i = 0; i < n; ++i) s += v[i] * v[i];
+  return std::sqrt(s);
+}
+double norm_inf(const double* v, size_t n) {
+  double s = 0.0;
+  for (size_t i = 0; i < n; ++i) s = std::max(s, std::fabs(v[i]));
+  return s;
+}
+
+}  // namespace
+
+// validate (src/preprocess.jl:8-74) for the LP descriptor, plus structural CSR checks
+// the reference gets from SparseMatrixCSC's invariants.
+void validate_lp_desc(const gpdhg_lp_desc* d) {
+  if (!d) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "descriptor is NULL");
+  if (d->num_variables <= 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "num_variables must be positive");
+  if (d->num_constraints < 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "num_constraints must be >= 0");
+  if (d->num_equalities < 0 || d->num_equalities > d->num_constraints)
+    throw Error(GPDHG_ERR_INVALID_PROBLEM, "num_equalities out of [0, num_constraints]");
+  if (!d->row_ptr || !d->variable_lower_bound || !d->variable_upper_bound || !d->objective_vector ||
+      (d->num_constraints > 0 && !d->right_hand_side))
+    throw Error(GPDHG_ERR_INVALID_ARGUMENT, "required array pointer is NULL");
+  const int32_t m = d->num_constraints, n = d->num_variables;
+  if (d->row_ptr[0] != 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "row_ptr[0] must be 0");
+  for (int32_t i = 0; i < m; ++i)
+    if (d->row_ptr[i + 1] < d->row_ptr[i]) throw Error(GPDHG_ERR_INVALID_PROBLEM, "row_ptr is not monotone");
+  const int64_t nnz = d->row_ptr[m];
+  if (nnz != d->nnz) throw Error(GPDHG_ERR_INVALID_PROBLEM, "nnz does not match row_ptr[m]");
+  if (nnz > 0 && (!d->col_idx || !d->values)) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "col_idx/values NULL");
+  for (int64_t k = 0; k < nnz; ++k) {
+    if (d->col_idx[k] < 0 || d->col_idx[k] >= n) throw Error(GPDHG_ERR_INVALID_PROBLEM, "column index out of range");
+    if (!std::isfinite(d->values[k])) throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN or Inf found in constraint matrix");
+  }
+  auto check_bounds = [&](const double* l, const double* u) {
+    for (int32_t j = 0; j < n; ++j) {
+      if (l[j] == INFINITY) throw Error(GPDHG_ERR_INVALID_PROBLEM, "variable_lower_bound contains +Inf");
+      if (u[j] == -INFINITY) throw Error(GPDHG_ERR_INVALID_PROBLEM, "variable_upper_bound contains -Inf");
+      if (std::isnan(l[j]) || std::isnan(u[j])) throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN found in variable bounds");
+    }
+  };
+  auto check_finite = [&](const double* v, int32_t len, const char* what) {
+    for (int32_t k = 0; k < len; ++k)
+      if (!std::isfinite(v[k])) throw Error(GPDHG_ERR_INVALID_PROBLEM, std::string("NaN or Inf found in ") + what);
+  };
+  check_bounds(d->variable_lower_bound, d->variable_upper_bound);
+  check_finite(d->objective_vector, n, "objective vector");
+  if (m) check_finite(d->right_hand_side, m, "right hand side");
+  if (!std::isfinite(d->objective_constant)) throw Error(GPDHG_ERR_INVALID_PROBLEM, "objective constant not finite");
+  if (d->original_variable_lower_bound && d->original_variable_upper_bound)
+    check_bounds(d->original_variable_lower_bound, d->original_variable_upper_bound);
+  if (d->original_objective_vector) check_finite(d->original_objective_vector, n, "original objective vector");
+  if (d->original_right_hand_side && m) check_finite(d->original_right_hand_side, m, "original right hand side");
+  auto check_pos = [&](const double* v, int32_t len, const char* what) {
+    for (int32_t k = 0; k < len; ++k)
+      if (!(v[k] > 0.0) || !std::isfinite(v[k]))
+        throw Error(GPDHG_ERR_INVALID_PROBLEM, std::string(what) + " must be positive and finite");
+  };
+  if (d->constraint_rescaling && m) check_pos(d->constraint_rescaling, m, "constraint_rescaling");
+  if (d->variable_rescaling) check_pos(d->variable_rescaling, n, "variable_rescaling");
+}
+
+void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d) {
+  validate_lp_desc(d);
+  const int32_t m = d->num_constraints, n = d->num_variables;
+  p->n = n;
+  p->m = m;
+  p->neq = d->num_equalities;
+  p->nnz = d->nnz;
+  p->obj_const = d->objective_constant;
+  CK(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+  cudaStream_t s = p->stream;
+
+  upload_matrix(p->A, m, n, d->row_ptr, d->col_idx, d->values, s);
+  HostCsr t;
+  transpose_csr(m, n, d->row_ptr, d->col_idx, d->values, t);
+  upload_matrix(p->At, n, m, t.row_ptr.data(), t.col.data(), t.val.data(), s);
+
+  std::vector<double> ones((size_t)std::max(m, n), 1.0);
+  upload_vec(p->l, d->variable_lower_bound, n, s);
+  upload_vec(p->u, d->variable_upper_bound, n, s);
+  upload_vec(p->c, d->objective_vector, n, s);
+  upload_vec(p->b, d->right_hand_side, m, s);
+  upload_vec_or_fill(p->ol, d->original_variable_lower_bound, d->variable_lower_bound, n, s);
+  upload_vec_or_fill(p->ou, d->original_variable_upper_bound, d->variable_upper_bound, n, s);
+  upload_vec_or_fill(p->oc, d->original_objective_vector, d->objective_vector, n, s);
+  upload_vec_or_fill(p->ob, d->original_right_hand_side, d->right_hand_side, m, s);
+  upload_vec_or_fill(p->con, d->constraint_rescaling, ones.data(), m, s);
+  upload_vec_or_fill(p->var, d->variable_rescaling, ones.data(), n, s);
+
+  double amax = 0.0;
+  for (int64_t k = 0; k < d->nnz; ++k) amax = std::max(amax, std::fabs(d->values[k]));
+  p->amax = amax;
+  p->norm2_c_scaled = norm2(d->objective_vector, n);
+  p->norm2_b_scaled = m ? norm2(d->right_hand_side, m) : 0.0;
+  const double* oc = d->original_objective_vector ? d->original_objective_vector : d->objective_vector;
+  const double* ob = d->original_right_hand_side ? d->original_right_hand_side : d->right_hand_side;
+  p->linf_c = norm_inf(oc, n);
+  p->l2_c = norm2(oc, n);
+  p->linf_b = m ? norm_inf(ob, m) : 0.0;
+  p->l2_b = m ? norm2(ob, m) : 0.0;
+  CK(cudaStreamSynchronize(s));
+}
+
+void ensure_fp32_values(gpdhg_problem* p) {
+  auto conv = [&](DeviceMatrix& dm) {
+    if (dm.val32.get()) return;
+    dm.val32.alloc(std::max<long long>(dm.nnz, 1));
+    if (dm.nnz) launch_convert_d2f(dm.val64.get(), dm.val32.get(), dm.nnz, p->stream);
+  };
+  conv(p->A);
+  conv(p->At);
+}
+
+}  // namespace gpdhg

@@ -1,0 +1,135 @@
+// problem.h — device layout of one LP and the solver workspaces.
+//
+// Replaces CuLinearProgrammingProblem / CuScaledQpProblem (src/cpu_to_gpu.jl:1-21):
+//   * scaled A as CSR (int32 row_ptr / col, FP64 values, FP32 values on demand),
+//   * explicit CSR of A' (the reference builds it with CuSparseMatrixCSR(A'), :46),
+//   * a row-block schedule for each (RowItem per CTA),
+//   * scaled l, u, c, b and the ORIGINAL l, u, c, b plus the two rescaling vectors,
+//     which is all the unscaled evaluation needs (the original matrix never is).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <vector>
+
+#include "common.cuh"
+
+namespace gpdhg {
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  explicit DBuf(size_t count) { alloc(count); }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) { reset(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DBuf() { reset(); }
+  void alloc(size_t count) {
+    reset();
+    n = count;
+    if (count) CK(cudaMalloc(&p, count * sizeof(T)));
+  }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  T* get() const { return p; }
+};
+
+template <class T>
+struct PinnedBuf {
+  T* p = nullptr;
+  PinnedBuf() = default;
+  explicit PinnedBuf(size_t count) { CK(cudaMallocHost(&p, count * sizeof(T) + 1)); }
+  PinnedBuf(const PinnedBuf&) = delete;
+  PinnedBuf& operator=(const PinnedBuf&) = delete;
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+};
+
+struct HostCsr {
+  std::vector<int32_t> row_ptr, col;
+  std::vector<double> val;
+};
+
+// Row-block schedule: consecutive rows packed while their nonzeros fit kItemNnz and
+// their count fits kRowsPerItem; a longer row gets an item of its own.
+std::vector<RowItem> build_row_items(const int32_t* row_ptr, int32_t nrows);
+
+// CSR of A' from CSR of A (counting sort, stable in row order).
+void transpose_csr(int32_t m, int32_t n, const int32_t* rp, const int32_t* col, const double* val, HostCsr& out);
+
+struct DeviceMatrix {
+  int32_t nrows = 0, ncols = 0;
+  long long nnz = 0;
+  DBuf<int32_t> row_ptr, col;
+  DBuf<double> val64;
+  DBuf<float> val32;
+  DBuf<RowItem> items;
+  int32_t num_items = 0;
+  template <class T>
+  CsrView<T> view() const;
+};
+
+template <>
+inline CsrView<double> DeviceMatrix::view<double>() const {
+  return CsrView<double>{nrows, ncols, row_ptr.get(), col.get(), val64.get(), items.get(), num_items};
+}
+template <>
+inline CsrView<float> DeviceMatrix::view<float>() const {
+  return CsrView<float>{nrows, ncols, row_ptr.get(), col.get(), val32.get(), items.get(), num_items};
+}
+
+template <class T>
+struct Workspace;
+// Out-of-line deleter so gpdhg_problem can be created where Workspace is incomplete.
+struct WorkspaceDeleter {
+  void operator()(Workspace<double>* w) const;
+  void operator()(Workspace<float>* w) const;
+};
+
+}  // namespace gpdhg
+
+struct gpdhg_problem {
+  int32_t n = 0, m = 0, neq = 0;
+  long long nnz = 0;
+  double obj_const = 0.0;
+  // host scalars derived once at creation
+  double amax = 0.0;              // max |a_ij| of the scaled matrix: tau_0 = 1 / amax (:571)
+  double norm2_c_scaled = 0.0;    // select_initial_primal_weight (src/saddle_point_gpu.jl:767-785)
+  double norm2_b_scaled = 0.0;
+  double linf_c = 0.0, linf_b = 0.0, l2_c = 0.0, l2_b = 0.0;  // CachedQuadraticProgramInfo (original)
+  gpdhg::DeviceMatrix A, At;
+  // scaled vectors (FP64; FP32 copies live in the FP32 workspace)
+  gpdhg::DBuf<double> l, u, c, b;
+  // original vectors and scaling
+  gpdhg::DBuf<double> ol, ou, oc, ob, con, var;
+  cudaStream_t stream = nullptr;
+  std::unique_ptr<gpdhg::Workspace<double>, gpdhg::WorkspaceDeleter> ws64;
+  std::unique_ptr<gpdhg::Workspace<float>, gpdhg::WorkspaceDeleter> ws32;
+  std::vector<gpdhg_iteration_stats> history;
+  std::vector<double> warm_x, warm_y;   // scaled warm start (empty: zero start)
+  int last_precision = -1;              // workspace holding the last current iterate
+  long long launches = 0;               // kernels launched on this handle so far
+  ~gpdhg_problem();
+};
+
+namespace gpdhg {
+// validate (src/preprocess.jl:8-74) plus CSR structure checks; throws gpdhg::Error.
+void validate_lp_desc(const gpdhg_lp_desc* d);
+// Builds the device problem from a descriptor (throws gpdhg::Error).
+void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d);
+// dst[k] = (float)src[k] on stream s.
+void launch_convert_d2f(const double* src, float* dst, long long n, cudaStream_t s);
+// Ensures FP32 copies of the matrix values exist.
+void ensure_fp32_values(gpdhg_problem* p);
+}  // namespace gpdhg

@@ -1,0 +1,22 @@
+// stubs.cu — entry points not implemented yet: they fail loudly with NOT_SUPPORTED.
+#include "problem.h"
+
+extern "C" {
+gpdhg_status gpdhg_problem_create_unscaled(const gpdhg_lp_desc*, const gpdhg_params*, gpdhg_problem** out) {
+  if (out) *out = nullptr;
+  return GPDHG_ERR_NOT_SUPPORTED;
+}
+gpdhg_status gpdhg_get_rescaling(const gpdhg_problem*, double*, double*) { return GPDHG_ERR_NOT_SUPPORTED; }
+gpdhg_status gpdhg_server_create(const gpdhg_server_config*, gpdhg_server** out) {
+  if (out) *out = nullptr;
+  return GPDHG_ERR_NOT_SUPPORTED;
+}
+gpdhg_status gpdhg_server_submit(gpdhg_server*, const gpdhg_lp_desc*, const gpdhg_params*, uint64_t*) {
+  return GPDHG_ERR_NOT_SUPPORTED;
+}
+gpdhg_status gpdhg_server_poll(gpdhg_server*, uint64_t, gpdhg_result*, double*, double*) { return GPDHG_ERR_NOT_SUPPORTED; }
+gpdhg_status gpdhg_server_wait(gpdhg_server*, uint64_t, double, gpdhg_result*, double*, double*) {
+  return GPDHG_ERR_NOT_SUPPORTED;
+}
+gpdhg_status gpdhg_server_destroy(gpdhg_server*) { return GPDHG_ERR_NOT_SUPPORTED; }
+}

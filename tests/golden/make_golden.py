@@ -1,0 +1,105 @@
+"""Generates tests/golden/golden.json: independent pins for the oracle and the library.
+
+cuPDLP.jl ships no golden vectors or known-answer tests for its solve loop (its only
+test runs MathOptInterface's conformance suite at rtol 1e-1), and it cannot run here.
+So the pins are:
+  * the planted optimum of each known-optimum instance (exact by construction);
+  * scipy.optimize.linprog(method="highs") optimal objectives, an independent FP64 solver;
+  * the oracle's own statistics at a fixed iteration count, so oracle regressions show,
+    with the same statistics from the oracle built with another summation order: their
+    distance is the round-off envelope within which two correct implementations agree.
+Each instance is re-generated from (generator, seed, sizes); a checksum of the
+generated data guards against a different numpy random stream.
+
+Run:  python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+import scipy.optimize as so
+import scipy.sparse as sp
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "cupdlp.jl_gb300"))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+import cupdlp  # noqa: E402
+from cupdlp import synthetic  # noqa: E402
+import oracle  # noqa: E402
+
+INSTANCES = [
+    {"gen": "known_optimum_lp", "seed": 0, "kw": {}},                                  # the plain FP64 workload
+    {"gen": "known_optimum_lp", "seed": 11, "kw": {"m": 200, "n": 400, "density": 0.03}},
+    {"gen": "known_optimum_lp", "seed": 12, "kw": {"m": 300, "n": 500, "neq": 300, "density": 0.02}},
+    {"gen": "known_optimum_lp", "seed": 13, "kw": {"m": 300, "n": 500, "neq": 0, "density": 0.02}},
+    {"gen": "transportation_lp", "seed": 14, "kw": {"supplies": 20, "demands": 80}},
+    {"gen": "transportation_lp", "seed": 15, "kw": {"supplies": 50, "demands": 200}},
+]
+
+
+def make(spec):
+    return getattr(synthetic, spec["gen"])(spec["seed"], **spec["kw"])
+
+
+def checksum(p):
+    a = sp.csc_matrix(p.constraint_matrix)
+    h = hashlib.sha256()
+    for arr in (a.indptr.astype(np.int64), a.indices.astype(np.int64), a.data, p.objective_vector,
+                p.right_hand_side, p.variable_lower_bound, p.variable_upper_bound):
+        h.update(np.ascontiguousarray(arr).tobytes())
+    return h.hexdigest()[:16]
+
+
+def highs_objective(p):
+    a = sp.csr_matrix(p.constraint_matrix)
+    neq = p.num_equalities
+    bounds = list(zip(np.where(np.isfinite(p.variable_lower_bound), p.variable_lower_bound, None),
+                      np.where(np.isfinite(p.variable_upper_bound), p.variable_upper_bound, None)))
+    res = so.linprog(p.objective_vector, A_ub=-a[neq:] if a.shape[0] > neq else None,
+                     b_ub=-p.right_hand_side[neq:] if a.shape[0] > neq else None,
+                     A_eq=a[:neq] if neq else None, b_eq=p.right_hand_side[:neq] if neq else None,
+                     bounds=bounds, method="highs")
+    assert res.status == 0, res.message
+    return float(res.fun) + p.objective_constant
+
+
+def main():
+    oracle.set_threads(8)
+    out = {"instances": []}
+    for spec in INSTANCES:
+        lp = make(spec)
+        p = lp.problem
+        entry = dict(spec)
+        entry["checksum"] = checksum(p)
+        entry["m"], entry["n"], entry["nnz"] = p.num_constraints, p.num_variables, int(p.constraint_matrix.nnz)
+        entry["planted_objective"] = lp.optimal_objective
+        entry["highs_objective"] = highs_objective(p)
+        params = cupdlp.default_parameters(tolerance=1e-8)
+        res, x, y, st = oracle.optimize(p, params)
+        ci = res.last_iteration_stats.convergence_information
+        entry["oracle_1e8"] = {"termination_reason": res.termination_reason, "iteration_count": res.iteration_count,
+                               "primal_objective": ci.primal_objective, "dual_objective": ci.dual_objective}
+        params = cupdlp.default_parameters(tolerance=1e-8, iteration_limit=100)
+        sq = cupdlp.rescale_problem(10, False, 1.0, 0, p)
+        pert = oracle.solve_scaled(sq, params, perturbed=True).result.last_iteration_stats.convergence_information
+        res, x, y, st = oracle.optimize(p, params)
+        ci = res.last_iteration_stats.convergence_information
+        entry["oracle_it100_perturbed"] = {"primal_objective": pert.primal_objective,
+                                           "l2_dual_residual": pert.l2_dual_residual}
+        entry["oracle_it100"] = {"primal_objective": ci.primal_objective, "dual_objective": ci.dual_objective,
+                                 "l2_primal_residual": ci.l2_primal_residual, "l2_dual_residual": ci.l2_dual_residual,
+                                 "step_size": res.last_iteration_stats.step_size,
+                                 "primal_weight": res.last_iteration_stats.primal_weight,
+                                 "kkt_passes": res.cumulative_kkt_matrix_passes}
+        out["instances"].append(entry)
+        print(entry["gen"], entry["seed"], entry["highs_objective"], entry["oracle_1e8"])
+    with open(os.path.join(HERE, "golden.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,97 @@
+"""CPU tests of libgpdhg.so: it builds for sm_103a, loads, exports every declared
+symbol, and rejects bad input before touching a GPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import cupdlp
+from cupdlp import _abi
+from cupdlp.solver import unscaled_desc
+
+import instances
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "gpdhg.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(gpdhg_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_header_declares_what_python_binds():
+    assert declared_functions() == sorted(_abi.SIGNATURES)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_abi_version(lib):
+    assert lib.gpdhg_abi_version() == _abi.ABI_VERSION
+
+
+def test_default_params_match_host_defaults(lib):
+    c = _abi.Params()
+    lib.gpdhg_default_params(C.byref(c))
+    h = cupdlp.params_to_c(cupdlp.default_parameters(tolerance=1e-4, time_sec_limit=3600.0))
+    for name, _ in _abi.Params._fields_:
+        if name in ("verbosity", "reserved"):
+            continue
+        assert getattr(c, name) == getattr(h, name), name
+
+
+def _create_err(lib, desc):
+    h = C.c_void_p()
+    st = lib.gpdhg_problem_create(desc.ref, C.byref(h))
+    return st, lib.gpdhg_last_error().decode()
+
+
+def test_rejects_nan_matrix_before_any_gpu_work(lib):
+    p, _ = instances.tiny()
+    d = unscaled_desc(p)
+    d.arrays["vals"][0] = np.nan
+    st, msg = _create_err(lib, d)
+    assert st == _abi.ERR_INVALID_PROBLEM and "constraint matrix" in msg
+
+
+def test_rejects_bad_column_index(lib):
+    p, _ = instances.tiny()
+    d = unscaled_desc(p)
+    d.arrays["cols"][0] = 5
+    st, msg = _create_err(lib, d)
+    assert st == _abi.ERR_INVALID_PROBLEM and "column index" in msg
+
+
+def test_rejects_infinite_lower_bound(lib):
+    p, _ = instances.tiny()
+    p.variable_lower_bound = np.array([np.inf])
+    st, msg = _create_err(lib, unscaled_desc(p))
+    assert st == _abi.ERR_INVALID_PROBLEM and "+Inf" in msg
+
+
+def test_rejects_zero_variables(lib):
+    p, _ = instances.tiny()
+    d = unscaled_desc(p)
+    d.desc.num_variables = 0
+    st, _ = _create_err(lib, d)
+    assert st == _abi.ERR_INVALID_PROBLEM
+
+
+def test_rejects_nnz_mismatch(lib):
+    p, _ = instances.tiny()
+    d = unscaled_desc(p)
+    d.desc.nnz = 7
+    st, msg = _create_err(lib, d)
+    assert st == _abi.ERR_INVALID_PROBLEM and "nnz" in msg
+
+
+def test_null_arguments(lib):
+    assert lib.gpdhg_problem_create(None, None) == _abi.ERR_INVALID_ARGUMENT
+    assert lib.gpdhg_solve(None, None, None, None, None) == _abi.ERR_INVALID_ARGUMENT
+    st = _abi.IterationStats()
+    assert lib.gpdhg_get_stats(None, 0, C.byref(st)) == _abi.ERR_INVALID_ARGUMENT
+    assert "NULL" in lib.gpdhg_last_error().decode()
