@@ -25,8 +25,7 @@ namespace gpdhg {
 namespace {
 
 using Clock = std::chrono::steady_clock;
-constexpr int kBatchGraphBig = 32;
-constexpr int kBatchGraphSmall = 8;
+constexpr int kBatchLevels = 6;   // graphs of 1, 2, ..., 32 [primal, dual] pairs
 
 template <class T>
 void alloc_all(std::initializer_list<DBuf<T>*> v, size_t n) {
@@ -103,11 +102,11 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
       trp[co + j + 1] = (int32_t)tcol.size();
     }
     d_begin[k] = (int32_t)a_items.size();
-    for (RowItem it : build_row_items(d.row_ptr, m)) a_items.push_back({it.row_begin + ro, it.row_end + ro});
-    if (m == 0) a_items.push_back({ro, ro});  // every instance owns a dual CTA: its decision runs there
+    for (RowItem it : build_row_items(d.row_ptr, m)) a_items.push_back({it.row_begin + ro, it.row_end + ro, it.group, it.mode});
+    if (m == 0) a_items.push_back({ro, ro, 1, kItemStaged});  // every instance owns a dual CTA: its decision runs there
     while ((int)a_inst.size() < (int)a_items.size()) a_inst.push_back(k);
     p_begin[k] = (int32_t)t_items.size();
-    for (RowItem it : build_row_items(t.row_ptr.data(), n)) t_items.push_back({it.row_begin + co, it.row_end + co});
+    for (RowItem it : build_row_items(t.row_ptr.data(), n)) t_items.push_back({it.row_begin + co, it.row_end + co, it.group, it.mode});
     while ((int)t_inst.size() < (int)t_items.size()) t_inst.push_back(k);
     auto app = [](std::vector<double>& dst, const double* src, const double* fb, int len) {
       const double* p = src ? src : fb;
@@ -215,7 +214,7 @@ struct BatchWorkspace {
   PinnedBuf<double> red_host;
   DBuf<uint8_t> flags;             // 4 x count: active, use_current, to_avg, restart
   PinnedBuf<uint8_t> flags_host;
-  cudaGraphExec_t g_big = nullptr, g_small = nullptr;
+  cudaGraphExec_t graphs[kBatchLevels] = {};
   long long launches = 0;
   DBuf<double> pow_table;
   double pow_r = -1.0, pow_g = -1.0;
@@ -262,29 +261,28 @@ struct BatchWorkspace {
     red_part.alloc((size_t)16 * std::max(B->nseg_n, B->nseg_m));
     red_out.alloc((size_t)count * 32);
     flags.alloc(4 * (size_t)count);
-    g_big = capture(kBatchGraphBig);
-    g_small = capture(kBatchGraphSmall);
+    for (int lv = 0; lv < kBatchLevels; ++lv) graphs[lv] = capture(1 << lv);
   }
   ~BatchWorkspace() {
-    if (g_big) cudaGraphExecDestroy(g_big);
-    if (g_small) cudaGraphExecDestroy(g_small);
+    for (cudaGraphExec_t g : graphs)
+      if (g) cudaGraphExecDestroy(g);
   }
   BatchIndex index() const {
     return BatchIndex{B->item_inst_p.get(), B->item_inst_d.get(), B->p_item_begin.get(), B->d_item_begin.get(),
                       B->row_off_d.get(), B->neq_d.get()};
   }
-  BatchPrimalArgs<T> pargs(int mode) {
-    return BatchPrimalArgs<T>{B->At.view<T>(), index(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(), skty.get(),
+  PrimalArgs<T> pargs(int mode) {
+    return PrimalArgs<T>{B->At.view<T>(), index(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(), skty.get(),
                               y0.get(), y1.get(), st_dev.get(), part_p.get(), mode, direct};
   }
-  BatchDualArgs<T> dargs(int mode) {
-    return BatchDualArgs<T>{B->A.view<T>(), index(), dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(),
+  DualArgs<T> dargs(int mode) {
+    return DualArgs<T>{B->A.view<T>(), index(), dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(),
                             sy.get(), skx.get(), st_dev.get(), part_p.get(), part_d.get(), B->A.num_items, mode,
                             direct};
   }
   void launch_pair(int mode) {
-    batch_primal_kernel<T><<<B->At.num_items, kBlock, 0, B->stream>>>(pargs(mode));
-    batch_dual_kernel<T><<<B->A.num_items, kBlock, 0, B->stream>>>(dargs(mode));
+    primal_step_kernel<T><<<B->At.num_items, kBlock, 0, B->stream>>>(pargs(mode));
+    dual_step_kernel<T><<<B->A.num_items, kBlock, 0, B->stream>>>(dargs(mode));
     launches += 2;
   }
   cudaGraphExec_t capture(int pairs) {
@@ -292,8 +290,8 @@ struct BatchWorkspace {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < pairs; ++k) {
-      batch_primal_kernel<T><<<B->At.num_items, kBlock, 0, s>>>(pargs(kStepNormal));
-      batch_dual_kernel<T><<<B->A.num_items, kBlock, 0, s>>>(dargs(kStepNormal));
+      primal_step_kernel<T><<<B->At.num_items, kBlock, 0, s>>>(pargs(kStepNormal));
+      dual_step_kernel<T><<<B->A.num_items, kBlock, 0, s>>>(dargs(kStepNormal));
     }
     cudaMemcpyAsync(st_host.p, st_dev.get(), sizeof(StepState) * count, cudaMemcpyDeviceToHost, s);
     CK(cudaStreamEndCapture(s, &g));
@@ -565,9 +563,10 @@ static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& 
       for (int k = 0; k < K; ++k)
         if (!retired[k] && !st[k].done) max_remaining = std::max(max_remaining, st[k].target_in_chunk - st[k].accepted_in_chunk);
       if (max_remaining == 0) break;
-      const bool big = max_remaining >= kBatchGraphBig / 2;
-      CK(cudaGraphLaunch(big ? W.g_big : W.g_small, s));
-      W.launches += 2 * (big ? kBatchGraphBig : kBatchGraphSmall);
+      int lv = 0;
+      while (lv + 1 < kBatchLevels && (1 << lv) < max_remaining) ++lv;
+      CK(cudaGraphLaunch(W.graphs[lv], s));
+      W.launches += 2 * (1 << lv);
       CK(cudaStreamSynchronize(s));
       bool all_done = true;
       for (int k = 0; k < K; ++k)

@@ -27,16 +27,19 @@ inline void cuda_check(cudaError_t e, const char* what, const char* file, int li
 #define CK_LAUNCH() ::gpdhg::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
 
 constexpr int kBlock = 256;          // threads per CTA of every row-block kernel
-constexpr int kRowsPerItem = kBlock; // at most one row per thread in an item
-constexpr int kItemNnz = 2048;       // nonzeros staged in shared memory per item
+constexpr int kStageDepth = 8;                // independent (col, val) loads per thread and item
+constexpr int kStage = kBlock * kStageDepth;  // nonzeros staged per item (2048)
 constexpr int kReduceBlocks = 304;   // 2 x 152 SMs for grid-stride reductions
 
-// One CTA's share of a CSR matrix: rows [row_begin, row_end). When the range holds a
-// single row with more than kItemNnz nonzeros the CTA streams it directly from global
-// memory ("long row"); otherwise the products are staged in shared memory first.
+// One CTA's share of a CSR matrix: rows [row_begin, row_end) and the schedule used for
+// them (see spmv.cuh): staged short rows reduced by groups of `group` lanes, warp-per-row
+// register accumulation, or one long row streamed by the whole CTA.
+enum ItemMode : int32_t { kItemStaged = 0, kItemWarps = 1, kItemLong = 2 };
 struct RowItem {
   int32_t row_begin;
   int32_t row_end;
+  int32_t group;
+  int32_t mode;
 };
 
 // A contiguous element range [begin, end) of one instance, reduced by one CTA of the
@@ -145,5 +148,23 @@ __device__ __forceinline__ float jmax(float a, float b) { return (a != a || b !=
 __device__ __forceinline__ float jmin(float a, float b) { return (a != a || b != b) ? a + b : (a < b ? a : b); }
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Streaming accesses (read or written once per pass): evict-first in L1 and L2, so the
+// vectors gathered by the next kernel stay resident in L2.
+template <class T>
+__device__ __forceinline__ T lds(const T* p) { return __ldcs(p); }
+template <class T>
+__device__ __forceinline__ void sts(T* p, T v) { __stcs(p, v); }
+
+// max / min of doubles on the integer pipe (GB300's FP64 pipe is the scarce resource):
+// for non-NaN values the sign-magnitude bit pattern maps to an order-preserving int64 key.
+__device__ __forceinline__ long long order_key(double v) {
+  const long long b = __double_as_longlong(v);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double imax(double a, double b) { return order_key(a) < order_key(b) ? b : a; }
+__device__ __forceinline__ double imin(double a, double b) { return order_key(b) < order_key(a) ? b : a; }
+__device__ __forceinline__ float imax(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ float imin(float a, float b) { return fminf(a, b); }
 
 }  // namespace gpdhg

@@ -8,18 +8,32 @@
 namespace gpdhg {
 
 std::vector<RowItem> build_row_items(const int32_t* rp, int32_t nrows) {
+  // Rows longer than the stage get a CTA each; runs of rows with >= kWarpRow nonzeros go
+  // warp-per-row (at most 32 rows, 4 passes of 8 warps, per item); the remaining short rows
+  // are packed while their nonzeros fit the stage and there are at most kBlock of them, with
+  // the largest power-of-two lane group (<= 32) that still gives every row its own group.
+  constexpr int64_t kWarpRow = 64;
   std::vector<RowItem> items;
+  auto len = [&](int32_t r) { return (int64_t)rp[r + 1] - rp[r]; };
   int32_t r = 0;
   while (r < nrows) {
-    const int32_t start = r;
-    const int64_t base = rp[r];
-    if ((int64_t)rp[r + 1] - base > kItemNnz) {
-      items.push_back({r, r + 1});
+    if (len(r) > kStage) {
+      items.push_back({r, r + 1, 0, kItemLong});
       ++r;
       continue;
     }
-    while (r < nrows && r - start < kRowsPerItem && (int64_t)rp[r + 1] - base <= kItemNnz) ++r;
-    items.push_back({start, r});
+    const int32_t start = r;
+    if (len(r) >= kWarpRow) {
+      while (r < nrows && r - start < 32 && len(r) >= kWarpRow && len(r) <= kStage) ++r;
+      items.push_back({start, r, 32, kItemWarps});
+      continue;
+    }
+    const int64_t base = rp[r];
+    while (r < nrows && r - start < kBlock && len(r) < kWarpRow && (int64_t)rp[r + 1] - base <= kStage) ++r;
+    const int rows = r - start;
+    int g = 1;
+    while (g < 32 && 2 * g * rows <= kBlock) g <<= 1;
+    items.push_back({start, r, g, kItemStaged});
   }
   return items;
 }
@@ -56,6 +70,7 @@ void upload_matrix(DeviceMatrix& dm, int32_t nrows, int32_t ncols, const int32_t
     CK(cudaMemcpyAsync(dm.val64.get(), val, sizeof(double) * dm.nnz, cudaMemcpyHostToDevice, s));
   }
   std::vector<RowItem> items = build_row_items(rp, nrows);
+  if (items.empty()) items.push_back({0, 0, 1, kItemStaged});  // no rows: one idle CTA still runs the step decision
   dm.num_items = (int32_t)items.size();
   dm.items.alloc(std::max<size_t>(items.size(), 1));
   if (!items.empty())

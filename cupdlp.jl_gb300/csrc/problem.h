@@ -61,8 +61,8 @@ struct HostCsr {
   std::vector<double> val;
 };
 
-// Row-block schedule: consecutive rows packed while their nonzeros fit kItemNnz and
-// their count fits kRowsPerItem; a longer row gets an item of its own.
+// Row-block schedule: consecutive rows packed while their nonzeros fit the SpMV stage
+// (kStage) and there are at most kBlock of them; a longer row gets an item of its own.
 std::vector<RowItem> build_row_items(const int32_t* row_ptr, int32_t nrows);
 
 // CSR of A' from CSR of A (counting sort, stable in row order).

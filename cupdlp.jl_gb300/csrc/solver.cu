@@ -37,13 +37,14 @@ void launch_convert_d2f(const double* src, float* dst, long long n, cudaStream_t
 }
 
 // Plain y = M x (warm start, power method, FP64 hand-off).
+struct NoPre {};
 template <class T>
 __global__ void __launch_bounds__(kBlock) spmv_kernel(CsrView<T> M, const T* __restrict__ x, T* y) {
-  __shared__ T prod[kItemNnz];
-  __shared__ T rowsum[kBlock];
-  __shared__ double red[32];
-  auto epi = [&](int i, T s) { y[i] = s; };
-  if ((int)blockIdx.x < M.num_items) row_block_spmv(M, x, blockIdx.x, prod, rowsum, red, epi);
+  __shared__ T stage[kStage];
+  __shared__ T wsum[kBlock / 32];
+  auto pre = [](int) { return NoPre{}; };
+  auto post = [&](int i, T s, const NoPre&) { y[i] = s; };
+  if ((int)blockIdx.x < M.num_items) spmv_item(M, x, blockIdx.x, stage, wsum, pre, post);
 }
 
 template <class T>
@@ -53,8 +54,14 @@ struct DotF {
   __device__ __forceinline__ void operator()(long long i, double* acc) const { acc[0] += (double)a[i] * (double)b[i]; }
 };
 
-constexpr int kGraphBig = 64;
-constexpr int kGraphSmall = 8;
+// Step graphs hold 1, 2, 4, ..., 64 [primal, dual] pairs; a chunk launches the smallest one
+// that covers the accepted steps still missing, so finished chunks waste almost no launches.
+constexpr int kGraphLevels = 7;
+inline int graph_level(int remaining) {
+  int lv = 0;
+  while (lv + 1 < kGraphLevels && (1 << lv) < remaining) ++lv;
+  return lv;
+}
 // Host table of the step-size factors (1 - (k+1)^-r, 1 + (k+1)^-g) of take_step!
 // (:405-407): the device reads it instead of evaluating two FP64 pow() per attempt in one
 // thread, and the values are the host libm's, as in the reference's host-side loop.
@@ -84,7 +91,7 @@ struct Workspace {
   DBuf<int32_t> seg_n_begin, seg_m_begin;
   DBuf<uint8_t> one;
   int nseg_n = 1, nseg_m = 1;
-  cudaGraphExec_t g_big = nullptr, g_small = nullptr;
+  cudaGraphExec_t graphs[kGraphLevels] = {};
   // profiled variants: an event between every pair of kernels
   std::vector<cudaEvent_t> pev;   // per-kernel timing events (params.profile_kernels)
   DBuf<double> pow_table;
@@ -92,6 +99,8 @@ struct Workspace {
   const int direct = sizeof(T) == sizeof(float) ? 1 : 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int nP = 1, nD = 1;
+  // the lone LP as a batch of one: instance ids and ranges for the step kernels
+  DBuf<int32_t> item_inst_p, item_inst_d, p_begin, d_begin, row_off, neq_d;
 
   explicit Workspace(gpdhg_problem* p) : P(p), n(p->n), m(p->m), st_host(1), red_host(64) {
     const size_t N = std::max(n, 1), M = std::max(m, 1);
@@ -113,8 +122,21 @@ struct Workspace {
     for (DBuf<T>* v : {&x, &dx, &kty, &sx, &skty, &ax, &agrad, &grad, &rx, &rgrad, &tmp_n}) v->alloc(N);
     for (DBuf<T>* v : {&y0, &y1, &kx0, &kx1, &sy, &skx, &ay, &akx, &ry, &rkx, &tmp_m}) v->alloc(M);
     st_dev.alloc(1);
-    nP = std::max(P->At.num_items, 1);
-    nD = std::max(P->A.num_items, 1);
+    nP = P->At.num_items;
+    nD = P->A.num_items;
+    {
+      auto up = [&](DBuf<int32_t>& d, const std::vector<int32_t>& v) {
+        d.alloc(v.size());
+        CK(cudaMemcpyAsync(d.get(), v.data(), sizeof(int32_t) * v.size(), cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+      };
+      up(item_inst_p, std::vector<int32_t>(nP, 0));
+      up(item_inst_d, std::vector<int32_t>(nD, 0));
+      up(p_begin, {0, nP});
+      up(d_begin, {0, nD});
+      up(row_off, {0, m});
+      up(neq_d, {P->neq});
+    }
     part_p.alloc(nP);
     part_d.alloc(2 * (size_t)nD);
     red_out.alloc(64);
@@ -141,8 +163,8 @@ struct Workspace {
     build_graphs();
   }
   ~Workspace() {
-    if (g_big) cudaGraphExecDestroy(g_big);
-    if (g_small) cudaGraphExecDestroy(g_small);
+    for (cudaGraphExec_t g : graphs)
+      if (g) cudaGraphExecDestroy(g);
     for (cudaEvent_t e : pev) cudaEventDestroy(e);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -153,13 +175,16 @@ struct Workspace {
   T* ycur_mut(int parity) { return parity ? y1.get() : y0.get(); }
   T* kxcur_mut(int parity) { return parity ? kx1.get() : kx0.get(); }
 
+  BatchIndex index() const {
+    return BatchIndex{item_inst_p.get(), item_inst_d.get(), p_begin.get(), d_begin.get(), row_off.get(), neq_d.get()};
+  }
   PrimalArgs<T> primal_args(int mode) {
-    return PrimalArgs<T>{P->At.view<T>(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(), skty.get(),
+    return PrimalArgs<T>{P->At.view<T>(), index(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(), skty.get(),
                          y0.get(), y1.get(), st_dev.get(), part_p.get(), mode, direct};
   }
   DualArgs<T> dual_args(int mode) {
-    return DualArgs<T>{P->A.view<T>(), dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(), sy.get(),
-                       skx.get(), P->neq, nP, st_dev.get(), part_p.get(), part_d.get(), mode, direct};
+    return DualArgs<T>{P->A.view<T>(), index(), dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(), sy.get(),
+                       skx.get(), st_dev.get(), part_p.get(), part_d.get(), nD, mode, direct};
   }
 
   void launch_pair(int mode, cudaStream_t s) {
@@ -185,8 +210,7 @@ struct Workspace {
     return ex;
   }
   void build_graphs() {
-    g_big = capture(kGraphBig);
-    g_small = capture(kGraphSmall);
+    for (int lv = 0; lv < kGraphLevels; ++lv) graphs[lv] = capture(1 << lv);
   }
   // The same pairs launched directly with an event between every two kernels, for
   // per-kernel CUDA-event timing (events recorded as graph nodes cannot be timed).
@@ -485,13 +509,13 @@ bool run_phase(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopS
     while (true) {
       const int remaining = st.target_in_chunk - st.accepted_in_chunk;
       const int attempts_before = st.attempts_in_chunk;
-      const bool big = remaining >= kGraphBig / 2;
+      const int lv = graph_level(remaining);
       CK(cudaEventRecord(W.ev0, s));
       if (prof)
-        W.launch_profiled(big ? kGraphBig : kGraphSmall);
+        W.launch_profiled(1 << lv);
       else
-        CK(cudaGraphLaunch(big ? W.g_big : W.g_small, s));
-      P->launches += 2 * (big ? kGraphBig : kGraphSmall);
+        CK(cudaGraphLaunch(W.graphs[lv], s));
+      P->launches += 2 * (1 << lv);
       CK(cudaEventRecord(W.ev1, s));
       CK(cudaStreamSynchronize(s));
       float ms = 0.f;

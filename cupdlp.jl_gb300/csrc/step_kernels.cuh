@@ -27,6 +27,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "spmv.cuh"
 
 namespace gpdhg {
 
@@ -48,108 +49,91 @@ __device__ __forceinline__ double block_sum_mixed(T v, double* sh) {
   return r;
 }
 
-__device__ __forceinline__ int floor_pow2(int v) { return 1 << (31 - __clz(v)); }
-
-// Row block of item `item` of M times xg; calls epi(row, row_sum) once per row.
-// Every thread of the CTA must call this (it synchronises).
-template <class T, class Epi>
-__device__ __forceinline__ void row_block_spmv(const CsrView<T>& M, const T* __restrict__ xg, int item,
-                                               T* prod, T* rowsum, double* red, Epi& epi) {
-  const int tid = threadIdx.x;
-  const RowItem it = M.items[item];
-  const int r0 = it.row_begin, r1 = it.row_end;
-  const int rows = r1 - r0;
-  const int s0 = M.row_ptr[r0];
-  const int s1 = M.row_ptr[r1];
-  const int cnt = s1 - s0;
-  if (cnt > kItemNnz) {
-    // long row: the whole CTA strides over it, then a fixed-order tree
-    T acc = T(0);
-    for (int e = s0 + tid; e < s1; e += kBlock) acc += M.val[e] * xg[M.col[e]];
-    acc = warp_sum(acc);
-    __syncthreads();
-    T* wsum = rowsum;  // reuse: 8 warp sums
-    if ((tid & 31) == 0) wsum[tid >> 5] = acc;
-    __syncthreads();
-    if (tid == 0) {
-      T s = T(0);
-      for (int w = 0; w < kBlock / 32; ++w) s += wsum[w];
-      epi(r0, s);
-    }
-    return;
-  }
-  for (int e = tid; e < cnt; e += kBlock) prod[e] = M.val[s0 + e] * xg[M.col[s0 + e]];
-  __syncthreads();
-  const int g = min(32, floor_pow2(kBlock / (rows > 0 ? rows : 1)));
-  const int grp = tid / g, lane = tid % g;
-  T acc = T(0);
-  if (grp < rows) {
-    const int a = M.row_ptr[r0 + grp] - s0, b = M.row_ptr[r0 + grp + 1] - s0;
-    for (int e = a + lane; e < b; e += g) acc += prod[e];
-  }
-  for (int o = g >> 1; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, g);
-  if (lane == 0 && grp < rows) rowsum[grp] = acc;
-  __syncthreads();
-  if (tid < rows) epi(r0 + tid, rowsum[tid]);
-  (void)red;
-}
+// Per-instance ranges of the packed layout (a lone LP is a batch of one).
+struct BatchIndex {
+  const int32_t* item_inst_p;  // instance of each A' item
+  const int32_t* item_inst_d;  // instance of each A item
+  const int32_t* p_item_begin; // first A' item of each instance (count + 1 entries)
+  const int32_t* d_item_begin; // first A item of each instance (count + 1 entries)
+  const int32_t* row_off;      // first packed row of each instance (count + 1)
+  const int32_t* neq;          // equality rows of each instance
+};
 
 template <class T>
 struct PrimalArgs {
   CsrView<T> At;   // CSR of A' (n rows)
+  BatchIndex bi;
   const T* c;
   const T* l;
   const T* u;
   T* x;
-  T* dx;
+  T* dx;           // dx, or x^ in direct mode
   T* kty;
   T* sx;
   T* skty;
   const T* y0;
   const T* y1;
-  const StepState* st;
-  double* part_p;  // one ||dx||^2 partial per CTA
+  const StepState* st;  // one per instance
+  double* part_p;       // one ||dx||^2 partial per CTA
   int mode;
   int direct;
 };
 
 template <class T>
-__global__ void __launch_bounds__(kBlock) primal_step_kernel(PrimalArgs<T> a) {
-  __shared__ T prod[kItemNnz];
-  __shared__ T rowsum[kBlock];
+struct PrimalPre {
+  T x, dx, sx, skty, c, l, u;
+};
+
+template <class T>
+__global__ void __launch_bounds__(kBlock, 4) primal_step_kernel(PrimalArgs<T> a) {
+  __shared__ T stage[kStage];
+  __shared__ T wsum[kBlock / 32];
   __shared__ double red[32];
-  const StepState* st = a.st;
+  const int item = blockIdx.x;
+  const StepState* st = a.st + a.bi.item_inst_p[item];
   if (st->done) return;
   const bool pending = st->pending_commit != 0;
   const bool commit_only = a.mode == kStepCommitOnly;
   if (commit_only && !pending) return;
+  const bool direct = a.direct != 0;
   const T w = (T)st->commit_weight;
   const T tto = (T)(st->tau / st->omega);  // step_size / primal_weight
   const T* ycur = st->parity ? a.y1 : a.y0;
-  const int item = blockIdx.x;
   T acc = T(0);
-  const bool direct = a.direct != 0;
-  auto candidate = [&](int j, T xv, T ktyv) {
-    T v = xv - tto * (a.c[j] - ktyv);
-    v = jmin(a.u[j], jmax(a.l[j], v));
+  auto candidate = [&](int j, T xv, T ktyv, T c, T l, T u) {
+    T v = xv - tto * (c - ktyv);
+    v = imin(u, imax(l, v));   // min(u, max(l, .)) (:192); NaN-free data is validated on entry
     const T d = v - xv;
-    a.dx[j] = direct ? v : d;
+    a.dx[j] = direct ? v : d;  // gathered by the dual kernel next: a normal (L2-resident) store
     acc += d * d;
   };
   if (pending) {
-    auto epi = [&](int j, T ktyv) {
-      const T xv = direct ? a.dx[j] : a.x[j] + a.dx[j];
-      a.x[j] = xv;
-      a.kty[j] = ktyv;
-      a.sx[j] += xv * w;
-      a.skty[j] += ktyv * w;
-      if (!commit_only) candidate(j, xv, ktyv);
+    auto pre = [&](int j) {
+      PrimalPre<T> p;
+      p.x = direct ? T(0) : lds(a.x + j);
+      p.dx = lds(a.dx + j);
+      p.sx = lds(a.sx + j);
+      p.skty = lds(a.skty + j);
+      if (!commit_only) {
+        p.c = lds(a.c + j);
+        p.l = lds(a.l + j);
+        p.u = lds(a.u + j);
+      }
+      return p;
     };
-    row_block_spmv(a.At, ycur, item, prod, rowsum, red, epi);
+    auto post = [&](int j, T ktyv, const PrimalPre<T>& p) {
+      const T xv = direct ? p.dx : p.x + p.dx;   // x += dx (:303)
+      sts(a.x + j, xv);
+      sts(a.kty + j, ktyv);                      // K'y = A'y (:307)
+      sts(a.sx + j, p.sx + xv * w);              // weighted sums (src/saddle_point_gpu.jl:137,182)
+      sts(a.skty + j, p.skty + ktyv * w);
+      if (!commit_only) candidate(j, xv, ktyv, p.c, p.l, p.u);
+    };
+    spmv_item(a.At, ycur, item, stage, wsum, pre, post);
   } else {
     const RowItem it = a.At.items[item];
-    const int j = it.row_begin + threadIdx.x;
-    if (j < it.row_end) candidate(j, a.x[j], a.kty[j]);
+    for (int j = it.row_begin + threadIdx.x; j < it.row_end; j += kBlock)
+      candidate(j, lds(a.x + j), lds(a.kty + j), lds(a.c + j), lds(a.l + j), lds(a.u + j));
   }
   if (commit_only) return;
   const double s = block_sum_mixed(acc, red);
@@ -159,6 +143,7 @@ __global__ void __launch_bounds__(kBlock) primal_step_kernel(PrimalArgs<T> a) {
 template <class T>
 struct DualArgs {
   CsrView<T> A;    // CSR of A (m rows)
+  BatchIndex bi;
   const T* dx;
   const T* b;
   T* y0;
@@ -167,13 +152,17 @@ struct DualArgs {
   T* kx1;
   T* sy;
   T* skx;
-  int neq;
-  int num_p_blocks;
   StepState* st;
   const double* part_p;
-  double* part_d;  // [interaction | ||dy||^2], gridDim.x each
+  double* part_d;  // [interaction | ||dy||^2], num_items each
+  int num_items;
   int mode;
   int direct;      // dx holds x^ and the row sums are K x^ (see above)
+};
+
+template <class T>
+struct DualPre {
+  T y, kx, b, sy, skx;
 };
 
 // Decision of take_step! for one attempt (thread 0 of the last CTA).
@@ -243,19 +232,19 @@ __device__ __forceinline__ void step_decision(StepState* st, double inter_signed
 }
 
 template <class T>
-__global__ void __launch_bounds__(kBlock) dual_step_kernel(DualArgs<T> a) {
-  __shared__ T prod[kItemNnz];
-  __shared__ T rowsum[kBlock];
+__global__ void __launch_bounds__(kBlock, 4) dual_step_kernel(DualArgs<T> a) {
+  __shared__ T stage[kStage];
+  __shared__ T wsum[kBlock / 32];
   __shared__ double red[32];
   __shared__ int is_last;
-  StepState* st = a.st;
+  const int item = blockIdx.x;
+  const int inst = a.bi.item_inst_d[item];
+  StepState* st = a.st + inst;
   if (st->done) return;
   const bool pending = st->pending_commit != 0;
   const bool commit_only = a.mode == kStepCommitOnly;
-  if (commit_only && !pending) {
-    // nothing to commit; the flag is already clear
-    return;
-  }
+  if (commit_only && !pending) return;
+  const bool direct = a.direct != 0;
   const T w = (T)st->commit_weight;
   const T od = (T)(st->omega * st->tau);  // primal_weight * step_size
   const int p = st->parity;
@@ -263,50 +252,56 @@ __global__ void __launch_bounds__(kBlock) dual_step_kernel(DualArgs<T> a) {
   T* ynew = p ? a.y0 : a.y1;
   const T* kxcur = p ? a.kx1 : a.kx0;
   T* kxnew = p ? a.kx0 : a.kx1;
-  const int item = blockIdx.x;
+  const int ineq_from = a.bi.row_off[inst] + a.bi.neq[inst];
   T acc_i = T(0), acc_d = T(0);
-  if (item < a.A.num_items) {
-    if (commit_only) {
-      const RowItem it = a.A.items[item];
-      const int i = it.row_begin + threadIdx.x;
-      if (i < it.row_end) {
-        a.sy[i] += ycur[i] * w;
-        a.skx[i] += kxcur[i] * w;
-      }
-    } else {
-      const bool direct = a.direct != 0;
-      auto epi = [&](int i, T rs) {
-        const T yv = ycur[i], kxv = kxcur[i];
-        if (pending) {
-          a.sy[i] += yv * w;
-          a.skx[i] += kxv * w;
-        }
-        const T kdx = direct ? rs - kxv : rs;
-        T v = yv + od * ((a.b[i] - T(2) * kdx) - kxv);
-        if (i >= a.neq) v = jmax(v, T(0));
-        const T d = v - yv;
-        ynew[i] = yv + d;
-        kxnew[i] = direct ? rs : kxv + kdx;
-        acc_i += kdx * d;
-        acc_d += d * d;
-      };
-      row_block_spmv(a.A, a.dx, item, prod, rowsum, red, epi);
+  if (commit_only) {
+    const RowItem it = a.A.items[item];
+    for (int i = it.row_begin + threadIdx.x; i < it.row_end; i += kBlock) {
+      a.sy[i] += ycur[i] * w;
+      a.skx[i] += kxcur[i] * w;
     }
+  } else {
+    auto pre = [&](int i) {
+      DualPre<T> q;
+      q.y = lds(ycur + i);
+      q.kx = lds(kxcur + i);
+      q.b = lds(a.b + i);
+      if (pending) {
+        q.sy = lds(a.sy + i);
+        q.skx = lds(a.skx + i);
+      }
+      return q;
+    };
+    auto post = [&](int i, T rs, const DualPre<T>& q) {
+      if (pending) {
+        sts(a.sy + i, q.sy + q.y * w);
+        sts(a.skx + i, q.skx + q.kx * w);
+      }
+      const T kdx = direct ? rs - q.kx : rs;
+      T v = q.y + od * ((q.b - T(2) * kdx) - q.kx);   // (:247), extrapolation coefficient 1
+      if (i >= ineq_from) v = imax(v, T(0));          // (:254)
+      const T d = v - q.y;
+      ynew[i] = q.y + d;                              // y += dy (:306); gathered by the next primal kernel
+      sts(kxnew + i, direct ? rs : q.kx + kdx);       // Kx += K dx (:304)
+      acc_i += kdx * d;
+      acc_d += d * d;
+    };
+    spmv_item(a.A, a.dx, item, stage, wsum, pre, post);
   }
-  double bi = 0.0, bd = 0.0;
   if (!commit_only) {
-    bi = block_sum_mixed(acc_i, red);
-    bd = block_sum_mixed(acc_d, red);
+    const double bi = block_sum_mixed(acc_i, red);
+    const double bd = block_sum_mixed(acc_d, red);
     if (threadIdx.x == 0) {
       a.part_d[item] = bi;
-      a.part_d[gridDim.x + item] = bd;
+      a.part_d[a.num_items + item] = bd;
     }
   }
+  const int d0 = a.bi.d_item_begin[inst], d1 = a.bi.d_item_begin[inst + 1];
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned prev = atomicAdd(&st->arrive, 1u);
-    is_last = (prev == gridDim.x - 1) ? 1 : 0;
+    is_last = (prev == (unsigned)(d1 - d0 - 1)) ? 1 : 0;
   }
   __syncthreads();
   if (!is_last) return;
@@ -318,13 +313,14 @@ __global__ void __launch_bounds__(kBlock) dual_step_kernel(DualArgs<T> a) {
     }
     return;
   }
-  // last CTA: fixed-order reduction of every CTA's partials
+  // the instance's last CTA: its partials in item order, then take_step!'s decision
   double si = 0.0, sd = 0.0, sx = 0.0;
-  for (int k = threadIdx.x; k < (int)gridDim.x; k += kBlock) {
+  for (int k = d0 + threadIdx.x; k < d1; k += kBlock) {
     si += __ldcg(a.part_d + k);
-    sd += __ldcg(a.part_d + gridDim.x + k);
+    sd += __ldcg(a.part_d + a.num_items + k);
   }
-  for (int k = threadIdx.x; k < a.num_p_blocks; k += kBlock) sx += __ldcg(a.part_p + k);
+  const int p0 = a.bi.p_item_begin[inst], p1 = a.bi.p_item_begin[inst + 1];
+  for (int k = p0 + threadIdx.x; k < p1; k += kBlock) sx += __ldcg(a.part_p + k);
   si = block_sum(si, red);
   sd = block_sum(sd, red);
   sx = block_sum(sx, red);
