@@ -12,6 +12,10 @@
 namespace gpdhg {
 void solve(gpdhg_problem* P, const gpdhg_params& prm, gpdhg_result* res, double* primal_out, double* dual_out);
 void current_iterate(const gpdhg_problem* P, double* x, double* y);
+void convergence_noalloc(int32_t n, int32_t m, int32_t neq, double obj_const, const double* l, const double* u,
+                         const double* c, const double* b, const double* x, const double* y, const double* ax,
+                         const double* aty, double eps_abs, double eps_rel, void* stream,
+                         gpdhg_convergence_information* out);
 }  // namespace gpdhg
 
 namespace {
@@ -191,6 +195,21 @@ gpdhg_status gpdhg_batch_solve(gpdhg_batch* b, const gpdhg_params* params, gpdhg
     if (params->step_size_policy != GPDHG_STEPSIZE_ADAPTIVE)
       throw gpdhg::Error(GPDHG_ERR_NOT_SUPPORTED, "batched solves use the adaptive step size");
     gpdhg::batch_solve(b, *params, results, primal_out, dual_out);
+  });
+}
+
+gpdhg_status gpdhg_convergence_noalloc(int32_t num_variables, int32_t num_constraints, int32_t num_equalities,
+                                       double objective_constant, const double* variable_lower_bound,
+                                       const double* variable_upper_bound, const double* objective_vector,
+                                       const double* right_hand_side, const double* primal, const double* dual,
+                                       const double* primal_product, const double* dual_product,
+                                       double eps_optimal_absolute, double eps_optimal_relative, void* stream,
+                                       gpdhg_convergence_information* out) {
+  return guarded([&] {
+    gpdhg::convergence_noalloc(num_variables, num_constraints, num_equalities, objective_constant,
+                               variable_lower_bound, variable_upper_bound, objective_vector, right_hand_side, primal,
+                               dual, primal_product, dual_product, eps_optimal_absolute, eps_optimal_relative, stream,
+                               out);
   });
 }
 

@@ -185,6 +185,8 @@ SIGNATURES = {
     "gpdhg_batch_solve": (C.c_int, [C.c_void_p, C.POINTER(Params), C.POINTER(Result),
                                     C.POINTER(_dp), C.POINTER(_dp)]),
     "gpdhg_batch_destroy": (C.c_int, [C.c_void_p]),
+    "gpdhg_convergence_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_double] + [_dp] * 8
+                                  + [C.c_double, C.c_double, C.c_void_p, C.POINTER(ConvergenceInformation)]),
     "gpdhg_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
     "gpdhg_server_submit": (C.c_int, [C.c_void_p, C.POINTER(LpDesc), C.POINTER(Params),
                                       C.POINTER(C.c_uint64)]),

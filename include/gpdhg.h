@@ -319,6 +319,29 @@ gpdhg_status gpdhg_batch_solve(gpdhg_batch* b, const gpdhg_params* params, gpdhg
 gpdhg_status gpdhg_batch_destroy(gpdhg_batch* b);
 
 /* ---------------------------------------------------------------------------------
+ * Allocation-free evaluation. No counterpart in the reference.
+ *
+ * The reference's termination statistics (ConvergenceInformation of
+ * compute_convergence_information) of a candidate (x, y) of an unscaled LP, for callers that
+ * may not allocate GPU memory when they want a solution checked: code recording a CUDA graph,
+ * or a host whose own memory pool owns the device. Every pointer except `out` is a DEVICE
+ * pointer the caller owns: bounds and objective (n), right-hand side (m), x (n), y (m),
+ * primal_product = A x (m), dual_product = A'y (n). `stream` is a cudaStream_t or NULL.
+ * The library allocates nothing: its scratch is one fixed device array of 608.3 KiB that
+ * every GPU loading the library holds until the process exits, so n and m are limited to
+ * 16,777,216 each (GPDHG_ERR_INVALID_ARGUMENT beyond). The first call on a device looks the
+ * array's address up (make it before any stream capture); calls that overlap on the GPU share
+ * the array and race.
+ * ------------------------------------------------------------------------------- */
+gpdhg_status gpdhg_convergence_noalloc(int32_t num_variables, int32_t num_constraints, int32_t num_equalities,
+                                       double objective_constant, const double* variable_lower_bound,
+                                       const double* variable_upper_bound, const double* objective_vector,
+                                       const double* right_hand_side, const double* primal, const double* dual,
+                                       const double* primal_product, const double* dual_product,
+                                       double eps_optimal_absolute, double eps_optimal_relative, void* stream,
+                                       gpdhg_convergence_information* out);
+
+/* ---------------------------------------------------------------------------------
  * Serving loop: continuous batching of arriving LPs. Requests are admitted by HBM
  * footprint, packed into free slots of a device-resident batch, advanced together,
  * retired when they terminate and back-filled by waiting requests.
