@@ -18,6 +18,7 @@
 
 #include "batch.h"
 #include "batch_kernels.cuh"
+#include "chunks.h"
 #include "host_logic.h"
 
 namespace gpdhg {
@@ -78,12 +79,12 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
   std::vector<double> aval, tval;
   acol.reserve(nnz_total); aval.reserve(nnz_total); tcol.reserve(nnz_total); tval.reserve(nnz_total);
   std::vector<RowItem> a_items, t_items;
-  std::vector<int32_t> a_inst, t_inst, d_begin(count + 1), p_begin(count + 1);
   std::vector<double> l, u, c, b, ol, ou, oc, ob, con, var;
   std::vector<uint8_t> ineq(std::max(M, 1), 0);
   for (int k = 0; k < count; ++k) {
     const gpdhg_lp_desc& d = descs[k];
     const int32_t m = d.num_constraints, n = d.num_variables, ro = B->row_off[k], co = B->col_off[k];
+    const int32_t nnz_a0 = (int32_t)acol.size(), nnz_t0 = (int32_t)tcol.size();
     for (int32_t i = 0; i < m; ++i) {
       for (int32_t e = d.row_ptr[i]; e < d.row_ptr[i + 1]; ++e) {
         acol.push_back(d.col_idx[e] + co);
@@ -101,13 +102,9 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
       }
       trp[co + j + 1] = (int32_t)tcol.size();
     }
-    d_begin[k] = (int32_t)a_items.size();
-    for (RowItem it : build_row_items(d.row_ptr, m)) a_items.push_back({it.row_begin + ro, it.row_end + ro, it.group, it.mode});
-    if (m == 0) a_items.push_back({ro, ro, 1, kItemStaged});  // every instance owns a dual CTA: its decision runs there
-    while ((int)a_inst.size() < (int)a_items.size()) a_inst.push_back(k);
-    p_begin[k] = (int32_t)t_items.size();
-    for (RowItem it : build_row_items(t.row_ptr.data(), n)) t_items.push_back({it.row_begin + co, it.row_end + co, it.group, it.mode});
-    while ((int)t_inst.size() < (int)t_items.size()) t_inst.push_back(k);
+    for (RowItem it : build_row_items(d.row_ptr, m)) a_items.push_back({it.row_begin + ro, it.row_end + ro, it.group, it.mode, it.nnz_begin + nnz_a0, it.nnz_count});
+    if (m == 0) a_items.push_back({ro, ro, 1, kItemStaged, nnz_a0, 0});  // every instance owns a dual CTA: its decision runs there
+    for (RowItem it : build_row_items(t.row_ptr.data(), n)) t_items.push_back({it.row_begin + co, it.row_end + co, it.group, it.mode, it.nnz_begin + nnz_t0, it.nnz_count});
     auto app = [](std::vector<double>& dst, const double* src, const double* fb, int len) {
       const double* p = src ? src : fb;
       if (p) dst.insert(dst.end(), p, p + len);
@@ -142,8 +139,6 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
     for (int32_t i = 0; i < m; ++i) { s2 += obb[i] * obb[i]; si = std::max(si, std::fabs(obb[i])); }
     qi.l2_b = std::sqrt(s2); qi.linf_b = si;
   }
-  d_begin[count] = (int32_t)a_items.size();
-  p_begin[count] = (int32_t)t_items.size();
 
   auto up_i = [&](DBuf<int32_t>& dst, const std::vector<int32_t>& v) {
     dst.alloc(std::max<size_t>(v.size(), 1));
@@ -158,6 +153,7 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
     dm.nrows = nrows;
     dm.ncols = ncols;
     dm.nnz = (long long)col.size();
+    dm.host_rp = rp;
     up_i(dm.row_ptr, rp);
     up_i(dm.col, col);
     up_d(dm.val64, val);
@@ -167,10 +163,6 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
   };
   up_items(B->A, M, N, arp, acol, aval, a_items);
   up_items(B->At, N, M, trp, tcol, tval, t_items);
-  up_i(B->item_inst_d, a_inst);
-  up_i(B->item_inst_p, t_inst);
-  up_i(B->d_item_begin, d_begin);
-  up_i(B->p_item_begin, p_begin);
   up_i(B->row_off_d, B->row_off);
   up_i(B->neq_d, B->neq);
   up_d(B->l, l); up_d(B->u, u); up_d(B->c, c); up_d(B->b, b);
@@ -212,6 +204,10 @@ struct BatchWorkspace {
   PinnedBuf<StepState> st_host;
   DBuf<double> part_p, part_d, red_part, red_out;
   PinnedBuf<double> red_host;
+  ChunkPlan<T> plan_p, plan_d;   // chunks of the packed A' and A, instance by instance
+  int grid_p = 1, grid_d = 1;
+  static constexpr int kSmemP = StageLayout<T, kPrimalSlots>::kTotal;
+  static constexpr int kSmemD = StageLayout<T, kDualSlots>::kTotal;
   DBuf<uint8_t> flags;             // 4 x count: active, use_current, to_avg, restart
   PinnedBuf<uint8_t> flags_host;
   cudaGraphExec_t graphs[kBatchLevels] = {};
@@ -256,8 +252,15 @@ struct BatchWorkspace {
     alloc_all<T>({&x, &dx, &kty, &sx, &skty, &ax, &agrad, &grad, &rx, &rgrad}, N);
     alloc_all<T>({&y0, &y1, &kx0, &kx1, &sy, &skx, &ay, &akx, &ry, &rkx}, M);
     st_dev.alloc(count);
-    part_p.alloc(std::max(B->At.num_items, 1));
-    part_d.alloc(2 * (size_t)std::max(B->A.num_items, 1));
+    CK(cudaMemsetAsync(st_dev.get(), 0, sizeof(StepState) * count, s));
+    build_chunk_plan(plan_p, B->At, B->col_off, {}, s);
+    std::vector<int32_t> ineq_from(count);
+    for (int k = 0; k < count; ++k) ineq_from[k] = B->row_off[k] + B->neq[k];
+    build_chunk_plan(plan_d, B->A, B->row_off, ineq_from, s);
+    grid_p = persistent_grid((const void*)primal_step_kernel<T>, kSmemP, plan_p.num);
+    grid_d = persistent_grid((const void*)dual_step_kernel<T>, kSmemD, plan_d.num);
+    part_p.alloc(plan_p.num);
+    part_d.alloc(2 * (size_t)plan_d.num);
     red_part.alloc((size_t)16 * std::max(B->nseg_n, B->nseg_m));
     red_out.alloc((size_t)count * 32);
     flags.alloc(4 * (size_t)count);
@@ -268,30 +271,29 @@ struct BatchWorkspace {
       if (g) cudaGraphExecDestroy(g);
   }
   BatchIndex index() const {
-    return BatchIndex{B->item_inst_p.get(), B->item_inst_d.get(), B->p_item_begin.get(), B->d_item_begin.get(),
-                      B->row_off_d.get(), B->neq_d.get()};
+    return BatchIndex{plan_p.inst_begin.get(), plan_d.inst_begin.get(), B->row_off_d.get(), B->neq_d.get()};
   }
   PrimalArgs<T> pargs(int mode) {
-    return PrimalArgs<T>{B->At.view<T>(), index(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(), skty.get(),
-                              y0.get(), y1.get(), st_dev.get(), part_p.get(), mode, direct};
+    return PrimalArgs<T>{plan_p.view(), index(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(), skty.get(),
+                         y0.get(), y1.get(), st_dev.get(), part_p.get(), mode, direct, count == 1};
   }
   DualArgs<T> dargs(int mode) {
-    return DualArgs<T>{B->A.view<T>(), index(), dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(),
-                            sy.get(), skx.get(), st_dev.get(), part_p.get(), part_d.get(), B->A.num_items, mode,
-                            direct};
+    return DualArgs<T>{plan_d.view(), index(), dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(),
+                       sy.get(), skx.get(), st_dev.get(), part_p.get(), part_d.get(), mode, direct, count == 1};
   }
-  void launch_pair(int mode) {
-    primal_step_kernel<T><<<B->At.num_items, kBlock, 0, B->stream>>>(pargs(mode));
-    dual_step_kernel<T><<<B->A.num_items, kBlock, 0, B->stream>>>(dargs(mode));
+  void launch_pair(int mode, cudaStream_t s) {
+    primal_step_kernel<T><<<grid_p, kBlock, kSmemP, s>>>(pargs(mode));
+    dual_step_kernel<T><<<grid_d, kBlock, kSmemD, s>>>(dargs(mode));
     launches += 2;
   }
+  void launch_pair(int mode) { launch_pair(mode, B->stream); }
   cudaGraphExec_t capture(int pairs) {
     cudaStream_t s = B->stream;
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < pairs; ++k) {
-      primal_step_kernel<T><<<B->At.num_items, kBlock, 0, s>>>(pargs(kStepNormal));
-      dual_step_kernel<T><<<B->A.num_items, kBlock, 0, s>>>(dargs(kStepNormal));
+      primal_step_kernel<T><<<grid_p, kBlock, kSmemP, s>>>(pargs(kStepNormal));
+      dual_step_kernel<T><<<grid_d, kBlock, kSmemD, s>>>(dargs(kStepNormal));
     }
     cudaMemcpyAsync(st_host.p, st_dev.get(), sizeof(StepState) * count, cudaMemcpyDeviceToHost, s);
     CK(cudaStreamEndCapture(s, &g));
@@ -568,6 +570,7 @@ static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& 
       CK(cudaGraphLaunch(W.graphs[lv], s));
       W.launches += 2 * (1 << lv);
       CK(cudaStreamSynchronize(s));
+      if (st[0].pipe_fault) throw Error(GPDHG_ERR_CUDA, "step kernel: a shared-memory copy did not complete");
       bool all_done = true;
       for (int k = 0; k < K; ++k)
         if (!retired[k] && !st[k].done) all_done = false;

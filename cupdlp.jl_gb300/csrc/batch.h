@@ -30,7 +30,7 @@ struct gpdhg_batch {
   std::vector<gpdhg::InstanceInfo> info;
   std::vector<double> amax, norm_b, norm_c;
   gpdhg::DeviceMatrix A, At;                   // block-diagonal CSR of A and A'
-  gpdhg::DBuf<int32_t> item_inst_p, item_inst_d, p_item_begin, d_item_begin, row_off_d, neq_d;
+  gpdhg::DBuf<int32_t> row_off_d, neq_d;
   gpdhg::DBuf<double> l, u, c, b, ol, ou, oc, ob, con, var;
   gpdhg::DBuf<uint8_t> ineq_flag;              // per packed row: a '>=' row
   gpdhg::DBuf<int32_t> col_inst, row_inst;     // instance of each packed column / row

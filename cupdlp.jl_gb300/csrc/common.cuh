@@ -40,6 +40,8 @@ struct RowItem {
   int32_t row_end;
   int32_t group;
   int32_t mode;
+  int32_t nnz_begin;   // row_ptr[row_begin]
+  int32_t nnz_count;   // row_ptr[row_end] - row_ptr[row_begin]
 };
 
 // A contiguous element range [begin, end) of one instance, reduced by one CTA of the
@@ -89,7 +91,8 @@ struct StepState {
   int attempts_in_chunk;
   int max_attempts_in_chunk;
   int constant_step;       // ConstantStepsizeParams: every attempt is accepted
-  unsigned int arrive;     // last-CTA counter of the dual kernel
+  unsigned int arrive;     // chunks of the dual kernel finished in this attempt
+  int pipe_fault;          // a step kernel's shared-memory copy never landed (instance 0 only)
   long long primal_spmv;   // attempts whose primal kernel also ran A'y (a commit)
   const double* pow_table; // [1-(k+1)^-r, 1+(k+1)^-g] for k < pow_table_len (device)
   long long pow_table_len;

@@ -8,32 +8,34 @@
 namespace gpdhg {
 
 std::vector<RowItem> build_row_items(const int32_t* rp, int32_t nrows) {
-  // Rows longer than the stage get a CTA each; runs of rows with >= kWarpRow nonzeros go
-  // warp-per-row (at most 32 rows, 4 passes of 8 warps, per item); the remaining short rows
-  // are packed while their nonzeros fit the stage and there are at most kBlock of them, with
-  // the largest power-of-two lane group (<= 32) that still gives every row its own group.
-  constexpr int64_t kWarpRow = 64;
+  // Rows with more than kCtaRow nonzeros get a CTA each (streamed, 8 loads per thread in
+  // flight). The other rows are packed in order while their nonzeros fit the stage and there
+  // are at most kBlock of them, whatever their lengths (splitting by length would fragment a
+  // power-law matrix into thousands of tiny items); such an item of at most 8 rows averaging
+  // >= 64 nonzeros runs warp-per-row, any other is staged, with the largest power-of-two lane
+  // group (<= 32) that still gives every row its own group.
+  constexpr int64_t kCtaRow = 256, kWarpRow = 64;
   std::vector<RowItem> items;
   auto len = [&](int32_t r) { return (int64_t)rp[r + 1] - rp[r]; };
   int32_t r = 0;
   while (r < nrows) {
-    if (len(r) > kStage) {
-      items.push_back({r, r + 1, 0, kItemLong});
+    if (len(r) > kCtaRow) {
+      items.push_back({r, r + 1, 0, kItemLong, rp[r], (int32_t)len(r)});
       ++r;
       continue;
     }
     const int32_t start = r;
-    if (len(r) >= kWarpRow) {
-      while (r < nrows && r - start < 32 && len(r) >= kWarpRow && len(r) <= kStage) ++r;
-      items.push_back({start, r, 32, kItemWarps});
+    const int64_t base = rp[r];
+    while (r < nrows && r - start < kBlock && len(r) <= kCtaRow && (int64_t)rp[r + 1] - base <= kStage) ++r;
+    const int rows = r - start;
+    const int64_t nnz = (int64_t)rp[r] - base;
+    if (rows <= kBlock / 32 && nnz >= kWarpRow * rows) {
+      items.push_back({start, r, 32, kItemWarps, rp[start], (int32_t)nnz});
       continue;
     }
-    const int64_t base = rp[r];
-    while (r < nrows && r - start < kBlock && len(r) < kWarpRow && (int64_t)rp[r + 1] - base <= kStage) ++r;
-    const int rows = r - start;
     int g = 1;
     while (g < 32 && 2 * g * rows <= kBlock) g <<= 1;
-    items.push_back({start, r, g, kItemStaged});
+    items.push_back({start, r, g, kItemStaged, rp[start], (int32_t)nnz});
   }
   return items;
 }
@@ -61,6 +63,7 @@ void upload_matrix(DeviceMatrix& dm, int32_t nrows, int32_t ncols, const int32_t
   dm.nrows = nrows;
   dm.ncols = ncols;
   dm.nnz = rp[nrows];
+  dm.host_rp.assign(rp, rp + (size_t)nrows + 1);
   dm.row_ptr.alloc((size_t)nrows + 1);
   dm.col.alloc(std::max<long long>(dm.nnz, 1));
   dm.val64.alloc(std::max<long long>(dm.nnz, 1));
@@ -70,7 +73,7 @@ void upload_matrix(DeviceMatrix& dm, int32_t nrows, int32_t ncols, const int32_t
     CK(cudaMemcpyAsync(dm.val64.get(), val, sizeof(double) * dm.nnz, cudaMemcpyHostToDevice, s));
   }
   std::vector<RowItem> items = build_row_items(rp, nrows);
-  if (items.empty()) items.push_back({0, 0, 1, kItemStaged});  // no rows: one idle CTA still runs the step decision
+  if (items.empty()) items.push_back({0, 0, 1, kItemStaged, 0, 0});  // no rows: one idle CTA still runs the step decision
   dm.num_items = (int32_t)items.size();
   dm.items.alloc(std::max<size_t>(items.size(), 1));
   if (!items.empty())

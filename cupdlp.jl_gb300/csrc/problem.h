@@ -34,7 +34,8 @@ struct DBuf {
   void alloc(size_t count) {
     reset();
     n = count;
-    if (count) CK(cudaMalloc(&p, count * sizeof(T)));
+    // 64 spare bytes: bulk copies round their end up to 16 bytes
+    if (count) CK(cudaMalloc(&p, count * sizeof(T) + 64));
   }
   void reset() {
     if (p) cudaFree(p);
@@ -76,6 +77,7 @@ struct DeviceMatrix {
   DBuf<float> val32;
   DBuf<RowItem> items;
   int32_t num_items = 0;
+  std::vector<int32_t> host_rp;   // row pointer on the host (chunk plans are built from it)
   template <class T>
   CsrView<T> view() const;
 };

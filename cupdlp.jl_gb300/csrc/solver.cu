@@ -23,9 +23,11 @@
 
 #include "batch.h"
 #include "batch_kernels.cuh"
+#include "chunks.h"
 #include "eval_kernels.cuh"
 #include "host_logic.h"
 #include "problem.h"
+#include "spmv.cuh"
 #include "step_kernels.cuh"
 
 namespace gpdhg {
@@ -41,10 +43,11 @@ struct NoPre {};
 template <class T>
 __global__ void __launch_bounds__(kBlock) spmv_kernel(CsrView<T> M, const T* __restrict__ x, T* y) {
   __shared__ T stage[kStage];
+  __shared__ T stage2[sizeof(T) == 8 ? kStage : 1];
   __shared__ T wsum[kBlock / 32];
   auto pre = [](int) { return NoPre{}; };
   auto post = [&](int i, T s, const NoPre&) { y[i] = s; };
-  if ((int)blockIdx.x < M.num_items) spmv_item(M, x, blockIdx.x, stage, wsum, pre, post);
+  if ((int)blockIdx.x < M.num_items) spmv_item(M, x, blockIdx.x, stage, stage2, wsum, pre, post);
 }
 
 template <class T>
@@ -98,9 +101,12 @@ struct Workspace {
   double pow_r = -1.0, pow_g = -1.0;
   const int direct = sizeof(T) == sizeof(float) ? 1 : 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  int nP = 1, nD = 1;
-  // the lone LP as a batch of one: instance ids and ranges for the step kernels
-  DBuf<int32_t> item_inst_p, item_inst_d, p_begin, d_begin, row_off, neq_d;
+  // chunk plans of A' (primal kernel) and A (dual kernel); the lone LP is a batch of one
+  ChunkPlan<T> plan_p, plan_d;
+  int grid_p = 1, grid_d = 1;
+  static constexpr int kSmemP = StageLayout<T, kPrimalSlots>::kTotal;
+  static constexpr int kSmemD = StageLayout<T, kDualSlots>::kTotal;
+  DBuf<int32_t> row_off, neq_d;
 
   explicit Workspace(gpdhg_problem* p) : P(p), n(p->n), m(p->m), st_host(1), red_host(64) {
     const size_t N = std::max(n, 1), M = std::max(m, 1);
@@ -122,23 +128,22 @@ struct Workspace {
     for (DBuf<T>* v : {&x, &dx, &kty, &sx, &skty, &ax, &agrad, &grad, &rx, &rgrad, &tmp_n}) v->alloc(N);
     for (DBuf<T>* v : {&y0, &y1, &kx0, &kx1, &sy, &skx, &ay, &akx, &ry, &rkx, &tmp_m}) v->alloc(M);
     st_dev.alloc(1);
-    nP = P->At.num_items;
-    nD = P->A.num_items;
+    CK(cudaMemsetAsync(st_dev.get(), 0, sizeof(StepState), s));
+    build_chunk_plan(plan_p, P->At, {0, n}, {}, s);
+    build_chunk_plan(plan_d, P->A, {0, m}, {P->neq}, s);
+    grid_p = persistent_grid((const void*)primal_step_kernel<T>, kSmemP, plan_p.num);
+    grid_d = persistent_grid((const void*)dual_step_kernel<T>, kSmemD, plan_d.num);
     {
       auto up = [&](DBuf<int32_t>& d, const std::vector<int32_t>& v) {
         d.alloc(v.size());
         CK(cudaMemcpyAsync(d.get(), v.data(), sizeof(int32_t) * v.size(), cudaMemcpyHostToDevice, s));
         CK(cudaStreamSynchronize(s));
       };
-      up(item_inst_p, std::vector<int32_t>(nP, 0));
-      up(item_inst_d, std::vector<int32_t>(nD, 0));
-      up(p_begin, {0, nP});
-      up(d_begin, {0, nD});
       up(row_off, {0, m});
       up(neq_d, {P->neq});
     }
-    part_p.alloc(nP);
-    part_d.alloc(2 * (size_t)nD);
+    part_p.alloc(plan_p.num);
+    part_d.alloc(2 * (size_t)plan_d.num);
     red_out.alloc(64);
     {
       std::vector<SegItem> it;
@@ -176,20 +181,26 @@ struct Workspace {
   T* kxcur_mut(int parity) { return parity ? kx1.get() : kx0.get(); }
 
   BatchIndex index() const {
-    return BatchIndex{item_inst_p.get(), item_inst_d.get(), p_begin.get(), d_begin.get(), row_off.get(), neq_d.get()};
+    return BatchIndex{plan_p.inst_begin.get(), plan_d.inst_begin.get(), row_off.get(), neq_d.get()};
   }
   PrimalArgs<T> primal_args(int mode) {
-    return PrimalArgs<T>{P->At.view<T>(), index(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(), skty.get(),
-                         y0.get(), y1.get(), st_dev.get(), part_p.get(), mode, direct};
+    return PrimalArgs<T>{plan_p.view(), index(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(), skty.get(),
+                         y0.get(), y1.get(), st_dev.get(), part_p.get(), mode, direct, 1};
   }
   DualArgs<T> dual_args(int mode) {
-    return DualArgs<T>{P->A.view<T>(), index(), dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(), sy.get(),
-                       skx.get(), st_dev.get(), part_p.get(), part_d.get(), nD, mode, direct};
+    return DualArgs<T>{plan_d.view(), index(), dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(), sy.get(),
+                       skx.get(), st_dev.get(), part_p.get(), part_d.get(), mode, direct, 1};
+  }
+  void launch_primal(int mode, cudaStream_t s) {
+    primal_step_kernel<T><<<grid_p, kBlock, kSmemP, s>>>(primal_args(mode));
+  }
+  void launch_dual(int mode, cudaStream_t s) {
+    dual_step_kernel<T><<<grid_d, kBlock, kSmemD, s>>>(dual_args(mode));
   }
 
   void launch_pair(int mode, cudaStream_t s) {
-    primal_step_kernel<T><<<nP, kBlock, 0, s>>>(primal_args(mode));
-    dual_step_kernel<T><<<nD, kBlock, 0, s>>>(dual_args(mode));
+    launch_primal(mode, s);
+    launch_dual(mode, s);
     P->launches += 2;
   }
 
@@ -198,8 +209,8 @@ struct Workspace {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < pairs; ++k) {
-      primal_step_kernel<T><<<nP, kBlock, 0, s>>>(primal_args(kStepNormal));
-      dual_step_kernel<T><<<nD, kBlock, 0, s>>>(dual_args(kStepNormal));
+      launch_primal(kStepNormal, s);
+      launch_dual(kStepNormal, s);
     }
     cudaMemcpyAsync(st_host.p, st_dev.get(), sizeof(StepState), cudaMemcpyDeviceToHost, s);
     cudaError_t e = cudaStreamEndCapture(s, &g);
@@ -223,9 +234,9 @@ struct Workspace {
     cudaStream_t s = P->stream;
     CK(cudaEventRecord(pev[0], s));
     for (int k = 0; k < pairs; ++k) {
-      primal_step_kernel<T><<<nP, kBlock, 0, s>>>(primal_args(kStepNormal));
+      launch_primal(kStepNormal, s);
       CK(cudaEventRecord(pev[2 * k + 1], s));
-      dual_step_kernel<T><<<nD, kBlock, 0, s>>>(dual_args(kStepNormal));
+      launch_dual(kStepNormal, s);
       CK(cudaEventRecord(pev[2 * k + 2], s));
     }
     CK_LAUNCH();
@@ -521,6 +532,7 @@ bool run_phase(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopS
       float ms = 0.f;
       CK(cudaEventElapsedTime(&ms, W.ev0, W.ev1));
       L.step_loop_sec += 1e-3 * ms;
+      if (st.pipe_fault) throw Error(GPDHG_ERR_CUDA, "step kernel: a shared-memory copy did not complete");
       if (prof) {
         const std::vector<cudaEvent_t>& ev = W.pev;
         const int did = st.attempts_in_chunk - attempts_before;

@@ -3,15 +3,16 @@
 // An item (one CTA) covers rows [row_begin, row_end); its `mode` picks the schedule:
 //   kItemStaged  short rows whose nonzeros fit the CTA's stage (kStage = 256 x 8), at most
 //                one row per group of `group` lanes (1..32) — steps 1-3 below;
-//   kItemWarps   rows of >= 64 nonzeros, one warp per row in passes of 8 rows: register
-//                accumulation (one FMA per nonzero, four independent loads per lane in flight),
-//                which costs half the FP64 instructions of staging;
+//   kItemWarps   up to 8 rows of >= 64 nonzeros, one warp per row: register accumulation
+//                (one FMA per nonzero, four independent loads per lane in flight);
 //   kItemLong    one row longer than the stage, streamed by the whole CTA.
 // Staged items:
 //   1. the row's own epilogue loads (`pre`) are issued first;
 //   2. every thread loads U (col, val) pairs of the item — fully unrolled, independent,
-//      coalesced — then issues its U gathers, and stages the products in shared memory:
-//      U loads in flight per thread instead of one dependent load chain per nonzero;
+//      coalesced — then issues its U gathers, and stages the products in shared memory
+//      (FP64 stages value and gathered entry apart, so the row sum is one FMA per nonzero on
+//      GB300's scarce FP64 pipe): U loads in flight per thread instead of one dependent load
+//      chain per nonzero;
 //   3. after one barrier each group sums its row from shared memory in a fixed order and
 //      its lane 0 runs the epilogue (`post`).
 // Matrix streams use evict-first loads so the gathered vector stays in L2. The reduction
@@ -47,10 +48,11 @@ __device__ __forceinline__ T warp_row_dot(const CsrView<T>& M, const T* __restri
   return warp_sum((a0 + a1) + (a2 + a3));
 }
 
-// Runs the item's rows. Every thread of the CTA must call it. `stage` holds kStage T.
+// Runs the item's rows. Every thread of the CTA must call it. `stage` holds kStage T, and
+// so does `stage2` when T is double (unused otherwise).
 template <class T, class Pre, class Post>
 __device__ __forceinline__ void spmv_item(const CsrView<T>& M, const T* __restrict__ xg, int item, T* stage,
-                                          T* wsum, Pre&& pre, Post&& post) {
+                                          T* stage2, T* wsum, Pre&& pre, Post&& post) {
   constexpr int U = kStageDepth;
   const RowItem it = M.items[item];
   const int tid = threadIdx.x;
@@ -121,14 +123,25 @@ __device__ __forceinline__ void spmv_item(const CsrView<T>& M, const T* __restri
 #pragma unroll
     for (int q = 0; q < U; ++q) {
       const int k = q * kBlock + tid;
-      if (k < cnt) stage[k] = v[q] * xg[c[q]];
+      if (k < cnt) {
+        if constexpr (sizeof(T) == 8) {
+          stage[k] = v[q];
+          stage2[k] = xg[c[q]];
+        } else {
+          stage[k] = v[q] * xg[c[q]];
+        }
+      }
     }
   }
   __syncthreads();
   T sum = T(0);
   if (r < it.row_end) {
     const int a = M.row_ptr[r] - s0, b = M.row_ptr[r + 1] - s0;
-    for (int k = a + lane; k < b; k += g) sum += stage[k];
+    if constexpr (sizeof(T) == 8) {
+      for (int k = a + lane; k < b; k += g) sum += stage[k] * stage2[k];
+    } else {
+      for (int k = a + lane; k < b; k += g) sum += stage[k];
+    }
   }
   sum = group_sum(sum, g);
   if (owner) post(r, sum, p);

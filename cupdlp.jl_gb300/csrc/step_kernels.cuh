@@ -9,14 +9,15 @@
 //   K'y = A' y and the four weighted sums (:297-319, src/saddle_point_gpu.jl:131-221);
 //   tau <- min((1-(k+1)^-0.3) limit, (1+(k+1)^-0.6) tau)                (:405-409)
 //
-// Here one attempt is two kernels and no host round trip:
-//   primal_step_kernel: [if the previous attempt was accepted] K'y = A' y (CSR of A'),
-//       x += dx, and the x / K'y weighted sums; then the next dx, and per-CTA ||dx||^2.
+// Here one attempt is two persistent kernels (pipe.cuh) and no host round trip:
+//   primal_step_kernel: [if the previous attempt was accepted] K'y = A' y (chunks of A'),
+//       x += dx, and the x / K'y weighted sums; then the next dx, and per-chunk ||dx||^2.
 //   dual_step_kernel:   [if the previous attempt was accepted] the y / Kx weighted sums;
-//       then K dx (CSR of A), the projected dual candidate, Kx + K dx into the other half of
-//       the double-buffered y / Kx, per-CTA interaction and ||dy||^2 partials; the last CTA
-//       to finish reduces all partials in a fixed order and takes the accept/reject and
-//       step-size decision, flipping the buffer parity on accept.
+//       then K dx (chunks of A), the projected dual candidate, Kx + K dx into the other half
+//       of the double-buffered y / Kx, per-chunk interaction and ||dy||^2 partials; the CTA
+//       that finishes an instance's last chunk reduces that instance's partials in chunk
+//       order and takes the accept/reject and step-size decision, flipping the buffer
+//       parity on accept.
 // So an accepted step costs exactly one pass over A and one over A'; a rejected attempt
 // costs one pass over A plus a streaming pass over the n-vectors.
 //
@@ -27,41 +28,28 @@
 #pragma once
 
 #include "common.cuh"
-#include "spmv.cuh"
+#include "pipe.cuh"
 
 namespace gpdhg {
 
 enum StepMode : int { kStepNormal = 0, kStepCommitOnly = 1 };
 
-// Per-thread accumulators in T, warp tree in T, across warps in FP64.
-template <class T>
-__device__ __forceinline__ double block_sum_mixed(T v, double* sh) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  v = warp_sum(v);
-  __syncthreads();
-  if (lane == 0) sh[wid] = (double)v;
-  __syncthreads();
-  double r = 0.0;
-  if (wid == 0) {
-    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
-    r = warp_sum(r);
-  }
-  return r;
-}
-
 // Per-instance ranges of the packed layout (a lone LP is a batch of one).
 struct BatchIndex {
-  const int32_t* item_inst_p;  // instance of each A' item
-  const int32_t* item_inst_d;  // instance of each A item
-  const int32_t* p_item_begin; // first A' item of each instance (count + 1 entries)
-  const int32_t* d_item_begin; // first A item of each instance (count + 1 entries)
-  const int32_t* row_off;      // first packed row of each instance (count + 1)
-  const int32_t* neq;          // equality rows of each instance
+  const int32_t* p_chunk_begin;  // first A' chunk of each instance (count + 1 entries)
+  const int32_t* d_chunk_begin;  // first A chunk of each instance (count + 1 entries)
+  const int32_t* row_off;        // first packed row of each instance (count + 1)
+  const int32_t* neq;            // equality rows of each instance
 };
+
+// Vector slots of the primal stage: pending commit / no pending commit.
+enum PrimalSlot { kPX = 0, kPDX = 1, kPKTY = 1, kPSX = 2, kPSKTY = 3, kPC = 4, kPL = 5, kPU = 6, kPrimalSlots = 7 };
+// Vector slots of the dual stage.
+enum DualSlot { kDY = 0, kDKX = 1, kDB = 2, kDSY = 3, kDSKX = 4, kDualSlots = 5 };
 
 template <class T>
 struct PrimalArgs {
-  CsrView<T> At;   // CSR of A' (n rows)
+  ChunkView<T> plan;   // chunks of A' (rows = variables)
   BatchIndex bi;
   const T* c;
   const T* l;
@@ -73,76 +61,16 @@ struct PrimalArgs {
   T* skty;
   const T* y0;
   const T* y1;
-  const StepState* st;  // one per instance
-  double* part_p;       // one ||dx||^2 partial per CTA
+  StepState* st;   // one per instance
+  double* part_p;  // one ||dx||^2 partial per chunk
   int mode;
   int direct;
+  int single;      // one instance: a finished solve returns at once
 };
-
-template <class T>
-struct PrimalPre {
-  T x, dx, sx, skty, c, l, u;
-};
-
-template <class T>
-__global__ void __launch_bounds__(kBlock, 4) primal_step_kernel(PrimalArgs<T> a) {
-  __shared__ T stage[kStage];
-  __shared__ T wsum[kBlock / 32];
-  __shared__ double red[32];
-  const int item = blockIdx.x;
-  const StepState* st = a.st + a.bi.item_inst_p[item];
-  if (st->done) return;
-  const bool pending = st->pending_commit != 0;
-  const bool commit_only = a.mode == kStepCommitOnly;
-  if (commit_only && !pending) return;
-  const bool direct = a.direct != 0;
-  const T w = (T)st->commit_weight;
-  const T tto = (T)(st->tau / st->omega);  // step_size / primal_weight
-  const T* ycur = st->parity ? a.y1 : a.y0;
-  T acc = T(0);
-  auto candidate = [&](int j, T xv, T ktyv, T c, T l, T u) {
-    T v = xv - tto * (c - ktyv);
-    v = imin(u, imax(l, v));   // min(u, max(l, .)) (:192); NaN-free data is validated on entry
-    const T d = v - xv;
-    a.dx[j] = direct ? v : d;  // gathered by the dual kernel next: a normal (L2-resident) store
-    acc += d * d;
-  };
-  if (pending) {
-    auto pre = [&](int j) {
-      PrimalPre<T> p;
-      p.x = direct ? T(0) : lds(a.x + j);
-      p.dx = lds(a.dx + j);
-      p.sx = lds(a.sx + j);
-      p.skty = lds(a.skty + j);
-      if (!commit_only) {
-        p.c = lds(a.c + j);
-        p.l = lds(a.l + j);
-        p.u = lds(a.u + j);
-      }
-      return p;
-    };
-    auto post = [&](int j, T ktyv, const PrimalPre<T>& p) {
-      const T xv = direct ? p.dx : p.x + p.dx;   // x += dx (:303)
-      sts(a.x + j, xv);
-      sts(a.kty + j, ktyv);                      // K'y = A'y (:307)
-      sts(a.sx + j, p.sx + xv * w);              // weighted sums (src/saddle_point_gpu.jl:137,182)
-      sts(a.skty + j, p.skty + ktyv * w);
-      if (!commit_only) candidate(j, xv, ktyv, p.c, p.l, p.u);
-    };
-    spmv_item(a.At, ycur, item, stage, wsum, pre, post);
-  } else {
-    const RowItem it = a.At.items[item];
-    for (int j = it.row_begin + threadIdx.x; j < it.row_end; j += kBlock)
-      candidate(j, lds(a.x + j), lds(a.kty + j), lds(a.c + j), lds(a.l + j), lds(a.u + j));
-  }
-  if (commit_only) return;
-  const double s = block_sum_mixed(acc, red);
-  if (threadIdx.x == 0) a.part_p[item] = s;
-}
 
 template <class T>
 struct DualArgs {
-  CsrView<T> A;    // CSR of A (m rows)
+  ChunkView<T> plan;   // chunks of A (rows = constraints)
   BatchIndex bi;
   const T* dx;
   const T* b;
@@ -154,16 +82,145 @@ struct DualArgs {
   T* skx;
   StepState* st;
   const double* part_p;
-  double* part_d;  // [interaction | ||dy||^2], num_items each
-  int num_items;
+  double* part_d;  // [interaction | ||dy||^2], one pair per chunk
   int mode;
   int direct;      // dx holds x^ and the row sums are K x^ (see above)
+  int single;
+};
+
+// Shared memory beyond the dynamic stage ring.
+template <class T>
+struct StepSmem {
+  uint64_t bars[kPipeStages];
+  StageHdr hdr[kPipeStages];
+  ScanSmem<T> scan;
+  double red[2 * (kBlock / 32)];
+  double red2[32];
+  int flag;
 };
 
 template <class T>
-struct DualPre {
-  T y, kx, b, sy, skx;
-};
+__global__ void __launch_bounds__(kBlock, 2) primal_step_kernel(PrimalArgs<T> a) {
+  using L = StageLayout<T, kPrimalSlots>;
+  extern __shared__ __align__(128) uint8_t ring_raw[];
+  __shared__ StepSmem<T> sm;
+  // StageLayout::kTotal has 128 spare bytes so the ring can start on a 128-byte boundary
+  uint8_t* ring = ring_raw + ((128u - (smem_addr(ring_raw) & 127u)) & 127u);
+  if (a.single && a.st->done) return;
+  const bool commit_only = a.mode == kStepCommitOnly;
+  const bool direct = a.direct != 0;
+  const int tid = threadIdx.x;
+  auto stage = [&](int s) { return ring + (size_t)s * L::kBytes; };
+  auto vec = [&](int s, int slot) { return reinterpret_cast<T*>(stage(s) + L::off_vec + slot * L::kVec); };
+
+  auto issue = [&](int, int s, const Chunk& ch, const StepScalars& v) {
+    StageHdr& h = sm.hdr[s];
+    h.ch = ch;
+    h.issued = 0;
+    if (v.done) return;
+    const int pending = v.pending;
+    if (commit_only && !pending) return;
+    h.pending = pending;
+    h.parity = v.parity;
+    h.s0 = v.w;
+    h.s1 = v.tau / v.omega;  // step_size / primal_weight
+    const int al = ch.row_begin & ~(L::V - 1);
+    const int cnt = ch.rows ? ((ch.row_begin + ch.rows + L::V - 1) & ~(L::V - 1)) - al : 0;
+    h.voff = ch.row_begin - al;
+    uint64_t* bar = &sm.bars[s];
+    const uint32_t vb = (uint32_t)(cnt * (int)sizeof(T));
+    const uint32_t mb = pending ? (uint32_t)blob_bytes<T>(ch.rows, ch.nnz) : 0u;
+    int nv;
+    if (pending) nv = (direct ? 3 : 4) + (commit_only ? 0 : 3);
+    else nv = 5;
+    mbar_arrive_expect_tx(bar, mb + (uint32_t)nv * vb);
+    if (mb) bulk_load_stream(stage(s), a.plan.blob + ch.blob, mb, bar, policy_evict_first());
+    if (pending) {
+      if (!direct) issue_vec(vec(s, kPX), a.x, al, cnt, bar);
+      issue_vec(vec(s, kPDX), a.dx, al, cnt, bar);
+      issue_vec(vec(s, kPSX), a.sx, al, cnt, bar);
+      issue_vec(vec(s, kPSKTY), a.skty, al, cnt, bar);
+    } else {
+      issue_vec(vec(s, kPX), a.x, al, cnt, bar);
+      issue_vec(vec(s, kPKTY), a.kty, al, cnt, bar);
+    }
+    if (!commit_only) {
+      issue_vec(vec(s, kPC), a.c, al, cnt, bar);
+      issue_vec(vec(s, kPL), a.l, al, cnt, bar);
+      issue_vec(vec(s, kPU), a.u, al, cnt, bar);
+    }
+    h.issued = 1;
+  };
+
+  auto gather = [&](int s) {
+    const StageHdr& h = sm.hdr[s];
+    if (!h.issued || !h.pending) return;
+    const int32_t* col = reinterpret_cast<const int32_t*>(stage(s) + blob_rp_bytes<T>(h.ch.rows));
+    T* xs = reinterpret_cast<T*>(stage(s) + L::off_xs);
+    const T* yg = h.parity ? a.y1 : a.y0;
+    for (int k = tid; k < h.ch.nnz; k += kBlock) gather_async(xs + pad_index(k, PipeTraits<T>::kPadShift), yg + col[k]);
+  };
+
+  auto compute = [&](int c, int s) {
+    const StageHdr& h = sm.hdr[s];
+    if (!h.issued) return;
+    const Chunk& ch = h.ch;
+    const T w = (T)h.s0;
+    const T tto = (T)h.s1;
+    T acc = T(0);
+    int slot = c;  // partial slot of this chunk's rows
+    auto candidate = [&](int j, T xv, T ktyv, T cv, T lv, T uv) {
+      T v = xv - tto * (cv - ktyv);
+      v = imin(uv, imax(lv, v));   // min(u, max(l, .)) (:192); NaN-free data is validated on entry
+      const T d = v - xv;
+      a.dx[j] = direct ? v : d;    // gathered by the dual kernel next: a normal (L2-resident) store
+      acc += d * d;
+    };
+    int rows = ch.rows;
+    if (h.pending) {
+      uint8_t* base = stage(s);
+      const int32_t* rp = reinterpret_cast<const int32_t*>(base);
+      const T* val = reinterpret_cast<const T*>(base + blob_rp_bytes<T>(ch.rows) + blob_col_bytes<T>(ch.nnz));
+      const T* xs = reinterpret_cast<const T*>(base + L::off_xs);
+      T* rs = reinterpret_cast<T*>(base + L::off_rs);
+      chunk_row_sums<T>(rp, val, xs, ch.rows, ch.nnz, ch.e_log2, rs, sm.scan);
+      __syncthreads();
+      if (ch.split >= 0) {
+        // a split row's contribution always lands in its first piece's slot, whichever
+        // piece finishes it, so the decision's reduction order does not depend on timing
+        if (tid == 0 && !commit_only) a.part_p[c] = 0.0;
+        if (!split_combine<T>(ch, a.plan, rs, &sm.flag)) return;
+        slot = c - ch.piece;
+      }
+      const T* vx = vec(s, kPX);
+      const T* vdx = vec(s, kPDX);
+      const T* vsx = vec(s, kPSX);
+      const T* vsk = vec(s, kPSKTY);
+      for (int r = tid; r < rows; r += kBlock) {
+        const int j = ch.row_begin + r, q = h.voff + r;
+        const T ktyv = rs[r];
+        const T xv = direct ? vdx[q] : vx[q] + vdx[q];   // x += dx (:303)
+        sts(a.x + j, xv);
+        sts(a.kty + j, ktyv);                            // K'y = A'y (:307)
+        sts(a.sx + j, vsx[q] + xv * w);                  // weighted sums (src/saddle_point_gpu.jl:137,182)
+        sts(a.skty + j, vsk[q] + ktyv * w);
+        if (!commit_only) candidate(j, xv, ktyv, vec(s, kPC)[q], vec(s, kPL)[q], vec(s, kPU)[q]);
+      }
+    } else {
+      if (ch.split >= 0 && ch.piece != ch.pieces - 1) rows = 0;
+      for (int r = tid; r < rows; r += kBlock) {
+        const int q = h.voff + r;
+        candidate(ch.row_begin + r, vec(s, kPX)[q], vec(s, kPKTY)[q], vec(s, kPC)[q], vec(s, kPL)[q], vec(s, kPU)[q]);
+      }
+    }
+    if (commit_only) return;
+    const double p = block_sum_1(acc, sm.red);
+    if (tid == 0) a.part_p[slot] = p;
+  };
+
+  if (!run_pipeline(a.plan.chunks, a.plan.num, a.st, sm.bars, sm.hdr, issue, gather, compute) && tid == 0)
+    atomicOr(&a.st->pipe_fault, 1);
+}
 
 // Decision of take_step! for one attempt (thread 0 of the last CTA).
 __device__ __forceinline__ void step_decision(StepState* st, double inter_signed, double dx2, double dy2) {
@@ -232,104 +289,176 @@ __device__ __forceinline__ void step_decision(StepState* st, double inter_signed
 }
 
 template <class T>
-__global__ void __launch_bounds__(kBlock, 4) dual_step_kernel(DualArgs<T> a) {
-  __shared__ T stage[kStage];
-  __shared__ T wsum[kBlock / 32];
-  __shared__ double red[32];
-  __shared__ int is_last;
-  const int item = blockIdx.x;
-  const int inst = a.bi.item_inst_d[item];
-  StepState* st = a.st + inst;
-  if (st->done) return;
-  const bool pending = st->pending_commit != 0;
+__global__ void __launch_bounds__(kBlock, 2) dual_step_kernel(DualArgs<T> a) {
+  using L = StageLayout<T, kDualSlots>;
+  extern __shared__ __align__(128) uint8_t ring_raw[];
+  __shared__ StepSmem<T> sm;
+  // StageLayout::kTotal has 128 spare bytes so the ring can start on a 128-byte boundary
+  uint8_t* ring = ring_raw + ((128u - (smem_addr(ring_raw) & 127u)) & 127u);
+  if (a.single && a.st->done) return;
   const bool commit_only = a.mode == kStepCommitOnly;
-  if (commit_only && !pending) return;
   const bool direct = a.direct != 0;
-  const T w = (T)st->commit_weight;
-  const T od = (T)(st->omega * st->tau);  // primal_weight * step_size
-  const int p = st->parity;
-  const T* ycur = p ? a.y1 : a.y0;
-  T* ynew = p ? a.y0 : a.y1;
-  const T* kxcur = p ? a.kx1 : a.kx0;
-  T* kxnew = p ? a.kx0 : a.kx1;
-  const int ineq_from = a.bi.row_off[inst] + a.bi.neq[inst];
-  T acc_i = T(0), acc_d = T(0);
-  if (commit_only) {
-    const RowItem it = a.A.items[item];
-    for (int i = it.row_begin + threadIdx.x; i < it.row_end; i += kBlock) {
-      a.sy[i] += ycur[i] * w;
-      a.skx[i] += kxcur[i] * w;
+  const int tid = threadIdx.x;
+  auto stage = [&](int s) { return ring + (size_t)s * L::kBytes; };
+  auto vec = [&](int s, int slot) { return reinterpret_cast<T*>(stage(s) + L::off_vec + slot * L::kVec); };
+
+  auto issue = [&](int, int s, const Chunk& ch, const StepScalars& v) {
+    StageHdr& h = sm.hdr[s];
+    h.ch = ch;
+    h.issued = 0;
+    if (v.done) return;
+    const int pending = v.pending;
+    if (commit_only && !pending) return;
+    h.pending = pending;
+    h.parity = v.parity;
+    h.s0 = v.w;
+    h.s1 = v.omega * v.tau;  // primal_weight * step_size
+    const int al = ch.row_begin & ~(L::V - 1);
+    const int cnt = ch.rows ? ((ch.row_begin + ch.rows + L::V - 1) & ~(L::V - 1)) - al : 0;
+    h.voff = ch.row_begin - al;
+    uint64_t* bar = &sm.bars[s];
+    const uint32_t vb = (uint32_t)(cnt * (int)sizeof(T));
+    const uint32_t mb = commit_only ? 0u : (uint32_t)blob_bytes<T>(ch.rows, ch.nnz);
+    const int nv = 2 + (commit_only ? 0 : 1) + (pending ? 2 : 0);
+    mbar_arrive_expect_tx(bar, mb + (uint32_t)nv * vb);
+    if (mb) bulk_load_stream(stage(s), a.plan.blob + ch.blob, mb, bar, policy_evict_first());
+    issue_vec(vec(s, kDY), h.parity ? a.y1 : a.y0, al, cnt, bar);
+    issue_vec(vec(s, kDKX), h.parity ? a.kx1 : a.kx0, al, cnt, bar);
+    if (!commit_only) issue_vec(vec(s, kDB), a.b, al, cnt, bar);
+    if (pending) {
+      issue_vec(vec(s, kDSY), a.sy, al, cnt, bar);
+      issue_vec(vec(s, kDSKX), a.skx, al, cnt, bar);
     }
-  } else {
-    auto pre = [&](int i) {
-      DualPre<T> q;
-      q.y = lds(ycur + i);
-      q.kx = lds(kxcur + i);
-      q.b = lds(a.b + i);
-      if (pending) {
-        q.sy = lds(a.sy + i);
-        q.skx = lds(a.skx + i);
+    h.issued = 1;
+  };
+
+  auto gather = [&](int s) {
+    const StageHdr& h = sm.hdr[s];
+    if (!h.issued || commit_only) return;
+    const int32_t* col = reinterpret_cast<const int32_t*>(stage(s) + blob_rp_bytes<T>(h.ch.rows));
+    T* xs = reinterpret_cast<T*>(stage(s) + L::off_xs);
+    for (int k = tid; k < h.ch.nnz; k += kBlock) gather_async(xs + pad_index(k, PipeTraits<T>::kPadShift), a.dx + col[k]);
+  };
+
+  // Arrivals are counted per CTA and instance: the CTA flushes its count when its chunk
+  // sequence moves to another instance and at the end, and the flush that completes the
+  // instance's chunk count takes take_step!'s decision for it.
+  int cur_inst = -1, cur_count = 0, cur_pending = 0;  // uniform across the CTA
+  auto flush = [&]() {
+    if (cur_count == 0) return;
+    const int inst = cur_inst;
+    StepState* st = a.st + inst;
+    const int d0 = a.bi.d_chunk_begin[inst], d1 = a.bi.d_chunk_begin[inst + 1];
+    if (tid == 0) {
+      __threadfence();
+      const unsigned prev = atomicAdd(&st->arrive, (unsigned)cur_count);
+      sm.flag = (prev + (unsigned)cur_count == (unsigned)(d1 - d0)) ? 1 : 0;
+    }
+    cur_count = 0;
+    __syncthreads();
+    if (!sm.flag) return;
+    __threadfence();
+    if (commit_only) {
+      if (tid == 0) {
+        st->pending_commit = 0;
+        st->arrive = 0;
       }
-      return q;
-    };
-    auto post = [&](int i, T rs, const DualPre<T>& q) {
-      if (pending) {
-        sts(a.sy + i, q.sy + q.y * w);
-        sts(a.skx + i, q.skx + q.kx * w);
+      return;
+    }
+    // the instance's partials in chunk order
+    double si = 0.0, sd = 0.0, sx = 0.0;
+    for (int k = d0 + tid; k < d1; k += kBlock) {
+      si += __ldcg(a.part_d + k);
+      sd += __ldcg(a.part_d + a.plan.num + k);
+    }
+    const int p0 = a.bi.p_chunk_begin[inst], p1 = a.bi.p_chunk_begin[inst + 1];
+    for (int k = p0 + tid; k < p1; k += kBlock) sx += __ldcg(a.part_p + k);
+    si = block_sum(si, sm.red2);
+    sd = block_sum(sd, sm.red2);
+    sx = block_sum(sx, sm.red2);
+    if (tid == 0) {
+      st->arrive = 0;
+      if (cur_pending) st->primal_spmv += 1;
+      st->pending_commit = 0;
+      step_decision(st, si, sx, sd);
+    }
+  };
+
+  auto compute = [&](int c, int s) {
+    const StageHdr& h = sm.hdr[s];
+    if (!h.issued) return;
+    const Chunk& ch = h.ch;
+    if (ch.inst != cur_inst) {
+      flush();
+      cur_inst = ch.inst;
+      cur_pending = h.pending;
+    }
+    ++cur_count;
+    const T w = (T)h.s0;
+    const T od = (T)h.s1;
+    const int p = h.parity;
+    T* ynew = p ? a.y0 : a.y1;
+    T* kxnew = p ? a.kx0 : a.kx1;
+    const T* vy = vec(s, kDY);
+    const T* vkx = vec(s, kDKX);
+    int rows = ch.rows;
+    if (commit_only) {
+      if (ch.split >= 0 && ch.piece != ch.pieces - 1) rows = 0;
+      for (int r = tid; r < rows; r += kBlock) {
+        const int i = ch.row_begin + r, q = h.voff + r;
+        sts(a.sy + i, vec(s, kDSY)[q] + vy[q] * w);
+        sts(a.skx + i, vec(s, kDSKX)[q] + vkx[q] * w);
       }
-      const T kdx = direct ? rs - q.kx : rs;
-      T v = q.y + od * ((q.b - T(2) * kdx) - q.kx);   // (:247), extrapolation coefficient 1
-      if (i >= ineq_from) v = imax(v, T(0));          // (:254)
-      const T d = v - q.y;
-      ynew[i] = q.y + d;                              // y += dy (:306); gathered by the next primal kernel
-      sts(kxnew + i, direct ? rs : q.kx + kdx);       // Kx += K dx (:304)
+      return;
+    }
+    const int ineq_from = ch.aux;
+    uint8_t* base = stage(s);
+    const int32_t* rp = reinterpret_cast<const int32_t*>(base);
+    const T* val = reinterpret_cast<const T*>(base + blob_rp_bytes<T>(ch.rows) + blob_col_bytes<T>(ch.nnz));
+    const T* xs = reinterpret_cast<const T*>(base + L::off_xs);
+    T* rs = reinterpret_cast<T*>(base + L::off_rs);
+    chunk_row_sums<T>(rp, val, xs, ch.rows, ch.nnz, ch.e_log2, rs, sm.scan);
+    __syncthreads();
+    int slot = c;
+    if (ch.split >= 0) {  // as in the primal kernel: the first piece's slot holds the row
+      if (tid == 0) {
+        a.part_d[c] = 0.0;
+        a.part_d[a.plan.num + c] = 0.0;
+      }
+      if (!split_combine<T>(ch, a.plan, rs, &sm.flag)) return;
+      slot = c - ch.piece;
+    }
+    T acc_i = T(0), acc_d = T(0);
+    const T* vb = vec(s, kDB);
+    for (int r = tid; r < rows; r += kBlock) {
+      const int i = ch.row_begin + r, q = h.voff + r;
+      const T y = vy[q], kx = vkx[q], rsum = rs[r];
+      if (h.pending) {
+        sts(a.sy + i, vec(s, kDSY)[q] + y * w);
+        sts(a.skx + i, vec(s, kDSKX)[q] + kx * w);
+      }
+      const T kdx = direct ? rsum - kx : rsum;
+      T v = y + od * ((vb[q] - T(2) * kdx) - kx);   // (:247), extrapolation coefficient 1
+      if (i >= ineq_from) v = imax(v, T(0));        // (:254)
+      const T d = v - y;
+      ynew[i] = y + d;                              // y += dy (:306); gathered by the next primal kernel
+      sts(kxnew + i, direct ? rsum : kx + kdx);     // Kx += K dx (:304)
       acc_i += kdx * d;
       acc_d += d * d;
-    };
-    spmv_item(a.A, a.dx, item, stage, wsum, pre, post);
-  }
-  if (!commit_only) {
-    const double bi = block_sum_mixed(acc_i, red);
-    const double bd = block_sum_mixed(acc_d, red);
-    if (threadIdx.x == 0) {
-      a.part_d[item] = bi;
-      a.part_d[a.num_items + item] = bd;
     }
-  }
-  const int d0 = a.bi.d_item_begin[inst], d1 = a.bi.d_item_begin[inst + 1];
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const unsigned prev = atomicAdd(&st->arrive, 1u);
-    is_last = (prev == (unsigned)(d1 - d0 - 1)) ? 1 : 0;
-  }
-  __syncthreads();
-  if (!is_last) return;
-  __threadfence();
-  if (commit_only) {
-    if (threadIdx.x == 0) {
-      st->pending_commit = 0;
-      st->arrive = 0;
+    double bi, bd;
+    block_sum_2(acc_i, acc_d, sm.red, bi, bd);
+    if (tid == 0) {
+      a.part_d[slot] = bi;
+      a.part_d[a.plan.num + slot] = bd;
     }
+  };
+
+  if (!run_pipeline(a.plan.chunks, a.plan.num, a.st, sm.bars, sm.hdr, issue, gather, compute)) {
+    if (tid == 0) atomicOr(&a.st->pipe_fault, 1);
     return;
   }
-  // the instance's last CTA: its partials in item order, then take_step!'s decision
-  double si = 0.0, sd = 0.0, sx = 0.0;
-  for (int k = d0 + threadIdx.x; k < d1; k += kBlock) {
-    si += __ldcg(a.part_d + k);
-    sd += __ldcg(a.part_d + a.num_items + k);
-  }
-  const int p0 = a.bi.p_item_begin[inst], p1 = a.bi.p_item_begin[inst + 1];
-  for (int k = p0 + threadIdx.x; k < p1; k += kBlock) sx += __ldcg(a.part_p + k);
-  si = block_sum(si, red);
-  sd = block_sum(sd, red);
-  sx = block_sum(sx, red);
-  if (threadIdx.x == 0) {
-    st->arrive = 0;
-    if (pending) st->primal_spmv += 1;
-    st->pending_commit = 0;
-    step_decision(st, si, sx, sd);
-  }
+  flush();
 }
 
 }  // namespace gpdhg
