@@ -18,7 +18,7 @@
 
 #include "batch.h"
 #include "batch_kernels.cuh"
-#include "chunks.h"
+#include "tiles.h"
 #include "host_logic.h"
 
 namespace gpdhg {
@@ -204,10 +204,8 @@ struct BatchWorkspace {
   PinnedBuf<StepState> st_host;
   DBuf<double> part_p, part_d, red_part, red_out;
   PinnedBuf<double> red_host;
-  ChunkPlan<T> plan_p, plan_d;   // chunks of the packed A' and A, instance by instance
-  int grid_p = 1, grid_d = 1;
-  static constexpr int kSmemP = StageLayout<T, kPrimalSlots>::kTotal;
-  static constexpr int kSmemD = StageLayout<T, kDualSlots>::kTotal;
+  TilePlan<T> plan_p, plan_d;   // tiles of the packed A' and A, instance by instance
+  DBuf<double> part_p_split, part_d_split;
   DBuf<uint8_t> flags;             // 4 x count: active, use_current, to_avg, restart
   PinnedBuf<uint8_t> flags_host;
   cudaGraphExec_t graphs[kBatchLevels] = {};
@@ -253,14 +251,14 @@ struct BatchWorkspace {
     alloc_all<T>({&y0, &y1, &kx0, &kx1, &sy, &skx, &ay, &akx, &ry, &rkx}, M);
     st_dev.alloc(count);
     CK(cudaMemsetAsync(st_dev.get(), 0, sizeof(StepState) * count, s));
-    build_chunk_plan(plan_p, B->At, B->col_off, {}, s);
+    build_tile_plan(plan_p, B->At, B->col_off, {}, s);
     std::vector<int32_t> ineq_from(count);
     for (int k = 0; k < count; ++k) ineq_from[k] = B->row_off[k] + B->neq[k];
-    build_chunk_plan(plan_d, B->A, B->row_off, ineq_from, s);
-    grid_p = persistent_grid((const void*)primal_step_kernel<T>, kSmemP, plan_p.num);
-    grid_d = persistent_grid((const void*)dual_step_kernel<T>, kSmemD, plan_d.num);
-    part_p.alloc(plan_p.num);
-    part_d.alloc(2 * (size_t)plan_d.num);
+    build_tile_plan(plan_d, B->A, B->row_off, ineq_from, s);
+    part_p.alloc(plan_p.num_ctas);
+    part_d.alloc(2 * (size_t)plan_d.num_ctas);
+    part_p_split.alloc(std::max(plan_p.num_splits, 1));
+    part_d_split.alloc(2 * (size_t)std::max(plan_d.num_splits, 1));
     red_part.alloc((size_t)16 * std::max(B->nseg_n, B->nseg_m));
     red_out.alloc((size_t)count * 32);
     flags.alloc(4 * (size_t)count);
@@ -270,20 +268,18 @@ struct BatchWorkspace {
     for (cudaGraphExec_t g : graphs)
       if (g) cudaGraphExecDestroy(g);
   }
-  BatchIndex index() const {
-    return BatchIndex{plan_p.inst_begin.get(), plan_d.inst_begin.get(), B->row_off_d.get(), B->neq_d.get()};
-  }
   PrimalArgs<T> pargs(int mode) {
-    return PrimalArgs<T>{plan_p.view(), index(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(), skty.get(),
-                         y0.get(), y1.get(), st_dev.get(), part_p.get(), mode, direct, count == 1};
+    return PrimalArgs<T>{B->At.view<T>(), plan_p.view(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(),
+                         skty.get(), y0.get(), y1.get(), st_dev.get(), part_p.get(), part_p_split.get(), mode, direct};
   }
   DualArgs<T> dargs(int mode) {
-    return DualArgs<T>{plan_d.view(), index(), dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(),
-                       sy.get(), skx.get(), st_dev.get(), part_p.get(), part_d.get(), mode, direct, count == 1};
+    return DualArgs<T>{B->A.view<T>(), plan_d.view(), plan_p.inst_cta_begin.get(), plan_p.inst_split_begin.get(),
+                       dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(), sy.get(), skx.get(), st_dev.get(),
+                       part_p.get(), part_p_split.get(), part_d.get(), part_d_split.get(), mode, direct};
   }
   void launch_pair(int mode, cudaStream_t s) {
-    primal_step_kernel<T><<<grid_p, kBlock, kSmemP, s>>>(pargs(mode));
-    dual_step_kernel<T><<<grid_d, kBlock, kSmemD, s>>>(dargs(mode));
+    primal_step_kernel<T><<<plan_p.num_ctas, kBlock, 0, s>>>(pargs(mode));
+    dual_step_kernel<T><<<plan_d.num_ctas, kBlock, 0, s>>>(dargs(mode));
     launches += 2;
   }
   void launch_pair(int mode) { launch_pair(mode, B->stream); }
@@ -292,8 +288,8 @@ struct BatchWorkspace {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < pairs; ++k) {
-      primal_step_kernel<T><<<grid_p, kBlock, kSmemP, s>>>(pargs(kStepNormal));
-      dual_step_kernel<T><<<grid_d, kBlock, kSmemD, s>>>(dargs(kStepNormal));
+      primal_step_kernel<T><<<plan_p.num_ctas, kBlock, 0, s>>>(pargs(kStepNormal));
+      dual_step_kernel<T><<<plan_d.num_ctas, kBlock, 0, s>>>(dargs(kStepNormal));
     }
     cudaMemcpyAsync(st_host.p, st_dev.get(), sizeof(StepState) * count, cudaMemcpyDeviceToHost, s);
     CK(cudaStreamEndCapture(s, &g));
@@ -570,7 +566,6 @@ static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& 
       CK(cudaGraphLaunch(W.graphs[lv], s));
       W.launches += 2 * (1 << lv);
       CK(cudaStreamSynchronize(s));
-      if (st[0].pipe_fault) throw Error(GPDHG_ERR_CUDA, "step kernel: a shared-memory copy did not complete");
       bool all_done = true;
       for (int k = 0; k < K; ++k)
         if (!retired[k] && !st[k].done) all_done = false;

@@ -91,8 +91,7 @@ struct StepState {
   int attempts_in_chunk;
   int max_attempts_in_chunk;
   int constant_step;       // ConstantStepsizeParams: every attempt is accepted
-  unsigned int arrive;     // chunks of the dual kernel finished in this attempt
-  int pipe_fault;          // a step kernel's shared-memory copy never landed (instance 0 only)
+  unsigned int arrive;     // CTAs of the dual kernel finished in this attempt
   long long primal_spmv;   // attempts whose primal kernel also ran A'y (a commit)
   const double* pow_table; // [1-(k+1)^-r, 1+(k+1)^-g] for k < pow_table_len (device)
   long long pow_table_len;

@@ -23,7 +23,7 @@
 
 #include "batch.h"
 #include "batch_kernels.cuh"
-#include "chunks.h"
+#include "tiles.h"
 #include "eval_kernels.cuh"
 #include "host_logic.h"
 #include "problem.h"
@@ -101,12 +101,9 @@ struct Workspace {
   double pow_r = -1.0, pow_g = -1.0;
   const int direct = sizeof(T) == sizeof(float) ? 1 : 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  // chunk plans of A' (primal kernel) and A (dual kernel); the lone LP is a batch of one
-  ChunkPlan<T> plan_p, plan_d;
-  int grid_p = 1, grid_d = 1;
-  static constexpr int kSmemP = StageLayout<T, kPrimalSlots>::kTotal;
-  static constexpr int kSmemD = StageLayout<T, kDualSlots>::kTotal;
-  DBuf<int32_t> row_off, neq_d;
+  // tile plans of A' (primal kernel) and A (dual kernel); the lone LP is a batch of one
+  TilePlan<T> plan_p, plan_d;
+  DBuf<double> part_p_split, part_d_split;
 
   explicit Workspace(gpdhg_problem* p) : P(p), n(p->n), m(p->m), st_host(1), red_host(64) {
     const size_t N = std::max(n, 1), M = std::max(m, 1);
@@ -129,21 +126,12 @@ struct Workspace {
     for (DBuf<T>* v : {&y0, &y1, &kx0, &kx1, &sy, &skx, &ay, &akx, &ry, &rkx, &tmp_m}) v->alloc(M);
     st_dev.alloc(1);
     CK(cudaMemsetAsync(st_dev.get(), 0, sizeof(StepState), s));
-    build_chunk_plan(plan_p, P->At, {0, n}, {}, s);
-    build_chunk_plan(plan_d, P->A, {0, m}, {P->neq}, s);
-    grid_p = persistent_grid((const void*)primal_step_kernel<T>, kSmemP, plan_p.num);
-    grid_d = persistent_grid((const void*)dual_step_kernel<T>, kSmemD, plan_d.num);
-    {
-      auto up = [&](DBuf<int32_t>& d, const std::vector<int32_t>& v) {
-        d.alloc(v.size());
-        CK(cudaMemcpyAsync(d.get(), v.data(), sizeof(int32_t) * v.size(), cudaMemcpyHostToDevice, s));
-        CK(cudaStreamSynchronize(s));
-      };
-      up(row_off, {0, m});
-      up(neq_d, {P->neq});
-    }
-    part_p.alloc(plan_p.num);
-    part_d.alloc(2 * (size_t)plan_d.num);
+    build_tile_plan(plan_p, P->At, {0, n}, {}, s);
+    build_tile_plan(plan_d, P->A, {0, m}, {P->neq}, s);
+    part_p.alloc(plan_p.num_ctas);
+    part_d.alloc(2 * (size_t)plan_d.num_ctas);
+    part_p_split.alloc(std::max(plan_p.num_splits, 1));
+    part_d_split.alloc(2 * (size_t)std::max(plan_d.num_splits, 1));
     red_out.alloc(64);
     {
       std::vector<SegItem> it;
@@ -180,22 +168,20 @@ struct Workspace {
   T* ycur_mut(int parity) { return parity ? y1.get() : y0.get(); }
   T* kxcur_mut(int parity) { return parity ? kx1.get() : kx0.get(); }
 
-  BatchIndex index() const {
-    return BatchIndex{plan_p.inst_begin.get(), plan_d.inst_begin.get(), row_off.get(), neq_d.get()};
-  }
   PrimalArgs<T> primal_args(int mode) {
-    return PrimalArgs<T>{plan_p.view(), index(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(), skty.get(),
-                         y0.get(), y1.get(), st_dev.get(), part_p.get(), mode, direct, 1};
+    return PrimalArgs<T>{P->At.view<T>(), plan_p.view(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(),
+                         skty.get(), y0.get(), y1.get(), st_dev.get(), part_p.get(), part_p_split.get(), mode, direct};
   }
   DualArgs<T> dual_args(int mode) {
-    return DualArgs<T>{plan_d.view(), index(), dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(), sy.get(),
-                       skx.get(), st_dev.get(), part_p.get(), part_d.get(), mode, direct, 1};
+    return DualArgs<T>{P->A.view<T>(), plan_d.view(), plan_p.inst_cta_begin.get(), plan_p.inst_split_begin.get(),
+                       dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(), sy.get(), skx.get(), st_dev.get(),
+                       part_p.get(), part_p_split.get(), part_d.get(), part_d_split.get(), mode, direct};
   }
   void launch_primal(int mode, cudaStream_t s) {
-    primal_step_kernel<T><<<grid_p, kBlock, kSmemP, s>>>(primal_args(mode));
+    primal_step_kernel<T><<<plan_p.num_ctas, kBlock, 0, s>>>(primal_args(mode));
   }
   void launch_dual(int mode, cudaStream_t s) {
-    dual_step_kernel<T><<<grid_d, kBlock, kSmemD, s>>>(dual_args(mode));
+    dual_step_kernel<T><<<plan_d.num_ctas, kBlock, 0, s>>>(dual_args(mode));
   }
 
   void launch_pair(int mode, cudaStream_t s) {
@@ -532,7 +518,6 @@ bool run_phase(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopS
       float ms = 0.f;
       CK(cudaEventElapsedTime(&ms, W.ev0, W.ev1));
       L.step_loop_sec += 1e-3 * ms;
-      if (st.pipe_fault) throw Error(GPDHG_ERR_CUDA, "step kernel: a shared-memory copy did not complete");
       if (prof) {
         const std::vector<cudaEvent_t>& ev = W.pev;
         const int did = st.attempts_in_chunk - attempts_before;

@@ -1,0 +1,115 @@
+// tiles.cu — host builder of the tile plans of the step kernels.
+#include <algorithm>
+
+#include "tiles.h"
+
+namespace gpdhg {
+
+namespace {
+int ceil_log2(long long v) {
+  int l = 0;
+  while ((1LL << l) < v) ++l;
+  return l;
+}
+}  // namespace
+
+void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t aux, std::vector<Tile>& out,
+                int32_t& splits, int32_t& carries) {
+  auto len = [&](int32_t r) { return (long long)rp[r + 1] - rp[r]; };
+  auto push = [&](int32_t rb, int32_t rows, long long nb, long long nnz, int32_t split, int32_t piece,
+                  int32_t pieces, int32_t carry) {
+    Tile t{};
+    t.row_begin = rb;
+    t.rows = rows;
+    t.nnz_begin = (int32_t)nb;
+    t.nnz = (int32_t)nnz;
+    // nonzeros per lane: enough for the tile, and about one row per lane when rows are
+    // short (fewer rows crossing lanes), at most kTileEMax
+    long long e = std::max<long long>(1, (nnz + 31) / 32);
+    if (rows > 0) e = std::max<long long>(e, std::min<long long>((nnz + rows - 1) / rows, kTileEMax));
+    t.e_log2 = ceil_log2(e);
+    t.split = split;
+    t.piece = piece;
+    t.pieces = pieces;
+    t.carry = carry;
+    t.aux = aux;
+    out.push_back(t);
+  };
+  const size_t first = out.size();
+  int32_t r = r0;
+  while (r < r1) {
+    const long long lr = len(r);
+    if (lr > kTileNnz) {
+      const int32_t pieces = (int32_t)((lr + kTileNnz - 1) / kTileNnz);
+      const int32_t sid = splits++;
+      const int32_t cb = carries;
+      carries += pieces;
+      for (int32_t q = 0; q < pieces; ++q)
+        push(r, 1, (long long)rp[r] + (long long)q * kTileNnz,
+             std::min<long long>(kTileNnz, lr - (long long)q * kTileNnz), sid, q, pieces, cb);
+      ++r;
+      continue;
+    }
+    const int32_t start = r;
+    long long nnz = 0;
+    while (r < r1 && r - start < kTileRows && len(r) <= kTileNnz && nnz + len(r) <= kTileNnz) {
+      nnz += len(r);
+      ++r;
+    }
+    push(start, r - start, rp[start], nnz, -1, 0, 1, 0);
+  }
+  if (out.size() == first) push(r0, 0, rp[r0], 0, -1, 0, 1, 0);
+}
+
+template <class T>
+void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector<int32_t>& bounds,
+                     const std::vector<int32_t>& aux, cudaStream_t s) {
+  if ((int32_t)M.host_rp.size() != M.nrows + 1) throw Error(GPDHG_ERR_INTERNAL, "matrix has no host row pointer");
+  const int K = (int)bounds.size() - 1;
+  std::vector<Tile> tiles;
+  std::vector<int32_t> cta_begin, cta_inst, inst_cta(K + 1), inst_split(K + 1);
+  int32_t splits = 0, carries = 0;
+  for (int k = 0; k < K; ++k) {
+    inst_cta[k] = (int32_t)cta_inst.size();
+    inst_split[k] = splits;
+    const size_t t0 = tiles.size();
+    list_tiles(M.host_rp.data(), bounds[k], bounds[k + 1], k, aux.empty() ? 0 : aux[k], tiles, splits, carries);
+    // CTAs: consecutive tiles of this instance, as even as possible; tiles per CTA grow
+    // from 8 to 32 once the instance has more than ~1,200 tiles (8 CTAs per SM of 152)
+    const long long nt = (long long)(tiles.size() - t0);
+    const long long tpc = std::min<long long>(kTilesPerCtaMax, std::max<long long>(kTilesPerCtaMin, (nt + 1215) / 1216));
+    const long long nc = (nt + tpc - 1) / tpc;
+    for (long long c = 0; c < nc; ++c) {
+      cta_begin.push_back((int32_t)(t0 + (nt * c) / nc));
+      cta_inst.push_back(k);
+    }
+  }
+  inst_cta[K] = (int32_t)cta_inst.size();
+  inst_split[K] = splits;
+  cta_begin.push_back((int32_t)tiles.size());
+  plan.num_tiles = (int32_t)tiles.size();
+  plan.num_ctas = (int32_t)cta_inst.size();
+  plan.num_splits = splits;
+  auto up = [&](DBuf<int32_t>& d, const std::vector<int32_t>& v) {
+    d.alloc(std::max<size_t>(v.size(), 1));
+    CK(cudaMemcpyAsync(d.get(), v.data(), sizeof(int32_t) * v.size(), cudaMemcpyHostToDevice, s));
+  };
+  plan.tiles.alloc(tiles.size());
+  CK(cudaMemcpyAsync(plan.tiles.get(), tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, s));
+  up(plan.cta_tile_begin, cta_begin);
+  up(plan.cta_inst, cta_inst);
+  up(plan.inst_cta_begin, inst_cta);
+  up(plan.inst_split_begin, inst_split);
+  plan.carry.alloc(std::max(carries, 1));
+  plan.counter.alloc(std::max(splits, 1));
+  CK(cudaMemsetAsync(plan.counter.get(), 0, sizeof(unsigned) * std::max(splits, 1), s));
+  // the host vectors die at return: wait for the copies before they do
+  CK(cudaStreamSynchronize(s));
+}
+
+template void build_tile_plan<float>(TilePlan<float>&, const DeviceMatrix&, const std::vector<int32_t>&,
+                                     const std::vector<int32_t>&, cudaStream_t);
+template void build_tile_plan<double>(TilePlan<double>&, const DeviceMatrix&, const std::vector<int32_t>&,
+                                      const std::vector<int32_t>&, cudaStream_t);
+
+}  // namespace gpdhg

@@ -1,0 +1,77 @@
+// tiles.h — the work decomposition of the step kernels: warp tiles grouped into CTAs.
+//
+// A tile is one warp's share of a CSR matrix: consecutive rows holding at most kTileNnz
+// nonzeros and at most kTileRows rows; a row longer than kTileNnz is cut into pieces of
+// kTileNnz, one tile each, whose partial sums meet in a carry array. Consecutive tiles of
+// one instance form a CTA's work (8 to 32 tiles, dealt to its 8 warps in turn), so
+// every CTA belongs to exactly one instance and the per-instance step decision can count
+// CTAs. An instance with few tiles gets one tile per warp (most CTAs in flight), a large one
+// up to four per warp (fewer partial sums for the step decision to reduce). The decomposition depends only on the instance's own row lengths, never on where
+// the instance sits in a packed batch.
+#pragma once
+
+#include <vector>
+
+#include "problem.h"
+
+namespace gpdhg {
+
+constexpr int kTileNnz = 256;     // nonzeros per tile (32 lanes x at most 8)
+constexpr int kTileRows = 31;     // rows per tile: rows + 1 row offsets fit in 32 lanes
+constexpr int kTileEMax = 8;      // nonzeros per lane
+constexpr int kTilesPerCtaMin = 8;   // tiles per CTA: one per warp for small instances,
+constexpr int kTilesPerCtaMax = 32;  // up to four per warp for large ones
+
+struct Tile {
+  int32_t row_begin;  // first row (packed numbering)
+  int32_t rows;       // rows of the tile (1 for a piece of a split row, 0 for an empty instance)
+  int32_t nnz_begin;  // first nonzero in the CSR
+  int32_t nnz;        // nonzeros of the tile
+  int32_t e_log2;     // log2 of the nonzeros per lane
+  int32_t split;      // -1, or the split row this piece belongs to
+  int32_t piece;      // piece index within the split row
+  int32_t pieces;     // pieces of the split row
+  int32_t carry;      // first carry slot of the split row
+  int32_t aux;        // tiles of A: first inequality row of the instance (packed numbering)
+};
+
+// Device view of a tile plan.
+template <class T>
+struct TileView {
+  const Tile* tiles;
+  const int32_t* cta_tile_begin;    // first tile of each CTA (ctas + 1)
+  const int32_t* cta_inst;          // instance of each CTA
+  const int32_t* inst_cta_begin;    // first CTA of each instance (instances + 1)
+  const int32_t* inst_split_begin;  // first split row of each instance (instances + 1)
+  T* carry;                         // one partial row sum per piece of every split row
+  unsigned* counter;                // pieces finished per split row (back to 0 after each launch)
+  int32_t num_ctas;
+  int32_t num_splits;
+};
+
+template <class T>
+struct TilePlan {
+  DBuf<Tile> tiles;
+  DBuf<int32_t> cta_tile_begin, cta_inst, inst_cta_begin, inst_split_begin;
+  DBuf<T> carry;
+  DBuf<unsigned> counter;
+  int32_t num_tiles = 0, num_ctas = 0, num_splits = 0;
+  TileView<T> view() const {
+    return TileView<T>{tiles.get(),      cta_tile_begin.get(), cta_inst.get(), inst_cta_begin.get(),
+                       inst_split_begin.get(), carry.get(),     counter.get(),  num_ctas,
+                       num_splits};
+  }
+};
+
+// Appends the tiles of rows [r0, r1) of a CSR with row pointer rp (instance inst). An empty
+// range still gets one empty tile (the instance's step decision runs in its CTA).
+void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t aux, std::vector<Tile>& out,
+                int32_t& splits, int32_t& carries);
+
+// Plan of rows [bounds[k], bounds[k + 1]) for every instance k of matrix M (Tile::aux =
+// aux[k], or 0 when aux is empty).
+template <class T>
+void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector<int32_t>& bounds,
+                     const std::vector<int32_t>& aux, cudaStream_t s);
+
+}  // namespace gpdhg

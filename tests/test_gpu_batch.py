@@ -30,7 +30,10 @@ def _mix(seed=21, count=12):
 @pytest.mark.parametrize("precision", [cupdlp.Precision.FP64, cupdlp.Precision.FP32])
 def test_batch_equals_alone_bitwise(precision):
     lps = _mix()
-    params = _params(tolerance=1e-6, precision=precision)
+    # FP32 runs at its own tolerance; the iteration limit keeps every instance's end
+    # independent of the wall clock, so the two runs must match exactly either way
+    tol = 1e-6 if precision == cupdlp.Precision.FP64 else 1e-4
+    params = _params(tolerance=tol, precision=precision, iteration_limit=100_000)
     scaled = [cupdlp.rescale_problem(10, False, 1.0, 0, lp.problem) for lp in lps]
     with DeviceBatch([scaled_desc(sq) for sq in scaled]) as db:
         results, xs, ys = db.solve(params)
