@@ -85,10 +85,24 @@ struct DualArgs {
   int direct;            // dx holds x^ and the row sums are K x^ (see above)
 };
 
+// One lane's epilogue inputs for its row of a tile (loaded one tile ahead).
+template <class T>
+struct PrimalIn {
+  T dx;  // dx (x^ in direct mode); K'y when no commit is pending
+  T x;
+  T sx;
+  T sk;
+  T c;
+  T l;
+  T u;
+};
+
 template <class T>
 __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_kernel(PrimalArgs<T> a) {
   __shared__ T rs_all[kBlock / 32][32];
   __shared__ double wsum[kBlock / 32];
+  __shared__ T wpart[kBlock / 32];
+  __shared__ Tile tl[kTilesPerCtaMax];
   const int b = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const StepState* st = a.st + a.plan.cta_inst[b];
   if (st->done) return;
@@ -96,53 +110,58 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_ke
   const bool commit_only = a.mode == kStepCommitOnly;
   if (commit_only && !pending) return;
   const bool direct = a.direct != 0;
+  // step_size / primal_weight: one FP64 division per CTA (GB300's FP64 pipe is narrow)
+  __shared__ double s_tto;
+  if (threadIdx.x == 0) s_tto = st->tau / st->omega;
+  const int nt = stage_tiles(a.plan.tiles, a.plan.cta_tile_begin[b], a.plan.cta_tile_begin[b + 1], tl);
   const T w = (T)st->commit_weight;
-  const T tto = (T)(st->tau / st->omega);  // step_size / primal_weight
+  const T tto = (T)s_tto;
   const T* yg = st->parity ? a.y1 : a.y0;
   T* rs = rs_all[warp];
   T acc = T(0);
-  // x^ = proj(x - (tau/omega)(c - K'y)) and dx (:177-197); returns ||dx||^2 of the entry
-  auto candidate = [&](int j, T xv, T ktyv, T cv, T lv, T uv) -> T {
-    T v = xv - tto * (cv - ktyv);
-    v = imin(uv, imax(lv, v));   // min(u, max(l, .)) (:192)
-    const T d = v - xv;
-    a.dx[j] = direct ? v : d;  // gathered by the dual kernel next: a normal (L2-resident) store
-    return d * d;
-  };
-  const int tb = a.plan.cta_tile_begin[b], te = a.plan.cta_tile_begin[b + 1];
-  for (int ti = tb + warp; ti < te; ti += kBlock / 32) {
-    const Tile t = a.plan.tiles[ti];
-    const bool split = t.split >= 0;
-    // this lane's row: its epilogue inputs are loaded before the row sums, so their latency
-    // overlaps that of the matrix and gather loads
+  auto load_in = [&](const Tile& t, PrimalIn<T>& e) {
+    e = PrimalIn<T>{};
+    if (lane >= t.rows) return;
     const int j = t.row_begin + lane;
-    const bool own = lane < t.rows;
-    T cv = T(0), lv = T(0), uv = T(0);
-    if (own && !commit_only) {
-      cv = lds(a.c + j);
-      lv = lds(a.l + j);
-      uv = lds(a.u + j);
+    if (!commit_only) {
+      e.c = lds(a.c + j);
+      e.l = lds(a.l + j);
+      e.u = lds(a.u + j);
     }
     if (pending) {
-      T dxv = T(0), x0 = T(0), sxv = T(0), skv = T(0);
-      if (own) {
-        dxv = lds(a.dx + j);
-        if (!direct) x0 = lds(a.x + j);
-        sxv = lds(a.sx + j);
-        skv = lds(a.skty + j);
-      }
-      tile_row_sums(a.At.row_ptr, a.At.col, a.At.val, yg, t, rs);
+      e.dx = lds(a.dx + j);
+      if (!direct) e.x = lds(a.x + j);
+      e.sx = lds(a.sx + j);
+      e.sk = lds(a.skty + j);
+    } else {
+      e.x = lds(a.x + j);
+      e.dx = lds(a.kty + j);
+    }
+  };
+  // x^ = proj(x - (tau/omega)(c - K'y)) and dx (:177-197); returns ||dx||^2 of the entry
+  auto candidate = [&](int j, T xv, T ktyv, const PrimalIn<T>& e) -> T {
+    T v = xv - tto * (e.c - ktyv);
+    v = imin(e.u, imax(e.l, v));   // min(u, max(l, .)) (:192)
+    const T d = v - xv;
+    a.dx[j] = direct ? v : d;      // gathered by the dual kernel next: a normal (L2-resident) store
+    return d * d;
+  };
+  // split handling and the fused epilogue of tile t, once its row sums are in rs
+  auto finish = [&](const Tile& t, const PrimalIn<T>& e) {
+    const bool split = t.split >= 0;
+    const int j = t.row_begin + lane;
+    if (pending) {
       int rows = t.rows;
       if (split) rows = split_finish(t, a.plan, rs) ? 1 : 0;
       if (lane < rows) {
         const T ktyv = rs[lane];
-        const T xv = direct ? dxv : x0 + dxv;   // x += dx (:303)
+        const T xv = direct ? e.dx : e.x + e.dx;   // x += dx (:303)
         sts(a.x + j, xv);
-        sts(a.kty + j, ktyv);                             // K'y = A'y (:307)
-        sts(a.sx + j, sxv + xv * w);                      // weighted sums (src/saddle_point_gpu.jl:137,182)
-        sts(a.skty + j, skv + ktyv * w);
+        sts(a.kty + j, ktyv);                       // K'y = A'y (:307)
+        sts(a.sx + j, e.sx + xv * w);               // weighted sums (src/saddle_point_gpu.jl:137,182)
+        sts(a.skty + j, e.sk + ktyv * w);
         if (!commit_only) {
-          const T d2 = candidate(j, xv, ktyv, cv, lv, uv);
+          const T d2 = candidate(j, xv, ktyv, e);
           if (split) {
             a.part_p_split[t.split] = (double)d2;
             __threadfence();
@@ -156,7 +175,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_ke
       // previous attempt rejected: K'y is unchanged, only the candidate is recomputed
       const int rows = (split && t.piece != t.pieces - 1) ? 0 : t.rows;
       if (lane < rows) {
-        const T d2 = candidate(j, lds(a.x + j), lds(a.kty + j), cv, lv, uv);
+        const T d2 = candidate(j, e.x, e.dx, e);
         if (split) {
           a.part_p_split[t.split] = (double)d2;
           __threadfence();
@@ -165,6 +184,27 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_ke
         }
       }
     }
+  };
+  TileLoad<T> L0;
+  PrimalIn<T> E0;
+  if (nt == 1 && tl[0].e_log2 == kCtaLong) {
+    // one long row for the whole CTA; warp 0 finishes it
+    const Tile t = tl[0];
+    if (warp == 0) load_in(t, E0);
+    if (pending) cta_row_sum(a.At.col, a.At.val, yg, t, wpart, &rs_all[0][0]);
+    if (warp == 0) finish(t, E0);
+  } else {
+    // each warp walks its tiles q = warp, warp + 8, ...: a tile's epilogue inputs, row
+    // offsets, columns and values are all issued before any of them is used
+    for (int q = warp; q < nt; q += kBlock / 32) {
+      const Tile t = tl[q];
+      load_in(t, E0);
+      if (pending) {
+        tile_load(a.At.row_ptr, a.At.col, a.At.val, t, L0);
+        tile_sums(a.At.col, a.At.val, yg, t, L0, rs);
+      }
+      finish(t, E0);
+    }
   }
   if (commit_only) return;
   const T ws = warp_sum(acc);
@@ -172,7 +212,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_ke
   __syncthreads();
   if (threadIdx.x == 0) {
     double p = 0.0;
-    for (int q = 0; q < kBlock / 32; ++q) p += wsum[q];
+    for (int k = 0; k < kBlock / 32; ++k) p += wsum[k];
     a.part_p[b] = p;
   }
 }
@@ -243,12 +283,24 @@ __device__ __forceinline__ void step_decision(StepState* st, double inter_signed
     st->done = 1;
 }
 
+// One lane's epilogue inputs for its row of a tile of A (loaded one tile ahead).
+template <class T>
+struct DualIn {
+  T y;
+  T kx;
+  T b;
+  T sy;
+  T sk;
+};
+
 template <class T>
 __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) dual_step_kernel(DualArgs<T> a) {
   __shared__ T rs_all[kBlock / 32][32];
   __shared__ double wsum[2][kBlock / 32];
   __shared__ double red[32];
   __shared__ int is_last;
+  __shared__ T wpart[kBlock / 32];
+  __shared__ Tile tl[kTilesPerCtaMax];
   const int b = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int inst = a.plan.cta_inst[b];
   StepState* st = a.st + inst;
@@ -257,8 +309,11 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) dual_step_kern
   const bool commit_only = a.mode == kStepCommitOnly;
   if (commit_only && !pending) return;
   const bool direct = a.direct != 0;
+  __shared__ double s_od;
+  if (threadIdx.x == 0) s_od = st->omega * st->tau;  // primal_weight * step_size
+  const int nt = stage_tiles(a.plan.tiles, a.plan.cta_tile_begin[b], a.plan.cta_tile_begin[b + 1], tl);
   const T w = (T)st->commit_weight;
-  const T od = (T)(st->omega * st->tau);  // primal_weight * step_size
+  const T od = (T)s_od;
   const int p = st->parity;
   const T* ycur = p ? a.y1 : a.y0;
   T* ynew = p ? a.y0 : a.y1;
@@ -266,46 +321,44 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) dual_step_kern
   T* kxnew = p ? a.kx0 : a.kx1;
   T* rs = rs_all[warp];
   T acc_i = T(0), acc_d = T(0);
-  const int tb = a.plan.cta_tile_begin[b], te = a.plan.cta_tile_begin[b + 1];
-  for (int ti = tb + warp; ti < te; ti += kBlock / 32) {
-    const Tile t = a.plan.tiles[ti];
+  auto load_in = [&](const Tile& t, DualIn<T>& e) {
+    e = DualIn<T>{};
+    if (lane >= t.rows) return;
+    const int i = t.row_begin + lane;
+    e.y = lds(ycur + i);
+    e.kx = lds(kxcur + i);
+    if (!commit_only) e.b = lds(a.b + i);
+    if (pending) {
+      e.sy = lds(a.sy + i);
+      e.sk = lds(a.skx + i);
+    }
+  };
+  auto finish = [&](const Tile& t, const DualIn<T>& e) {
     const bool split = t.split >= 0;
+    const int i = t.row_begin + lane;
     if (commit_only) {
       const int rows = (split && t.piece != t.pieces - 1) ? 0 : t.rows;
       if (lane < rows) {
-        const int i = t.row_begin + lane;
-        sts(a.sy + i, lds(a.sy + i) + lds(ycur + i) * w);
-        sts(a.skx + i, lds(a.skx + i) + lds(kxcur + i) * w);
+        sts(a.sy + i, e.sy + e.y * w);
+        sts(a.skx + i, e.sk + e.kx * w);
       }
-      continue;
+      return;
     }
-    // this lane's row: epilogue inputs first (their latency overlaps the row sums')
-    const int i = t.row_begin + lane;
-    T y = T(0), kx = T(0), bv = T(0), syv = T(0), skv = T(0);
-    if (lane < t.rows) {
-      y = lds(ycur + i);
-      kx = lds(kxcur + i);
-      bv = lds(a.b + i);
-      if (pending) {
-        syv = lds(a.sy + i);
-        skv = lds(a.skx + i);
-      }
-    }
-    tile_row_sums(a.A.row_ptr, a.A.col, a.A.val, a.dx, t, rs);
     int rows = t.rows;
     if (split) rows = split_finish(t, a.plan, rs) ? 1 : 0;
     if (lane < rows) {
       const T rsum = rs[lane];
+      const T y = e.y, kx = e.kx;
       if (pending) {
-        sts(a.sy + i, syv + y * w);
-        sts(a.skx + i, skv + kx * w);
+        sts(a.sy + i, e.sy + y * w);
+        sts(a.skx + i, e.sk + kx * w);
       }
       const T kdx = direct ? rsum - kx : rsum;
-      T v = y + od * ((bv - T(2) * kdx) - kx);   // (:247), extrapolation coefficient 1
-      if (i >= t.aux) v = imax(v, T(0));        // (:254)
+      T v = y + od * ((e.b - T(2) * kdx) - kx);   // (:247), extrapolation coefficient 1
+      if (i >= t.aux) v = imax(v, T(0));          // (:254)
       const T d = v - y;
-      ynew[i] = y + d;                          // y += dy (:306); gathered by the next primal kernel
-      sts(kxnew + i, direct ? rsum : kx + kdx); // Kx += K dx (:304)
+      ynew[i] = y + d;                            // y += dy (:306); gathered by the next primal kernel
+      sts(kxnew + i, direct ? rsum : kx + kdx);   // Kx += K dx (:304)
       if (split) {
         a.part_d_split[2 * t.split] = (double)(kdx * d);
         a.part_d_split[2 * t.split + 1] = (double)(d * d);
@@ -316,6 +369,24 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) dual_step_kern
       }
     }
     __syncwarp();
+  };
+  TileLoad<T> L0;
+  DualIn<T> E0;
+  if (nt == 1 && tl[0].e_log2 == kCtaLong) {
+    const Tile t = tl[0];
+    if (warp == 0) load_in(t, E0);
+    if (!commit_only) cta_row_sum(a.A.col, a.A.val, a.dx, t, wpart, &rs_all[0][0]);
+    if (warp == 0) finish(t, E0);
+  } else {
+    for (int q = warp; q < nt; q += kBlock / 32) {
+      const Tile t = tl[q];
+      load_in(t, E0);
+      if (!commit_only) {
+        tile_load(a.A.row_ptr, a.A.col, a.A.val, t, L0);
+        tile_sums(a.A.col, a.A.val, a.dx, t, L0, rs);
+      }
+      finish(t, E0);
+    }
   }
   if (!commit_only) {
     const T wi = warp_sum(acc_i), wd = warp_sum(acc_d);

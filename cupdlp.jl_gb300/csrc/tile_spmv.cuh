@@ -6,40 +6,122 @@
 
 namespace gpdhg {
 
-// Row sums of tile t: rs[r] = sum of val * xg[col] over row t.row_begin + r, r < t.rows.
-// Lane l takes the tile's nonzeros [l E, (l + 1) E), E = 2^e_log2, and issues all their
-// column, value and gathered-entry loads before using any (up to 3 E independent loads in
-// flight per lane), then sums them per row with one FMA per nonzero. The row offsets live
-// in the lanes' registers (lane i holds rp[i]) and are read with shuffles; a row that
-// crosses lanes is completed by a segmented shuffle scan of the lanes' trailing partial
-// sums. Every sum's order depends only on the tile, so the result does not depend on the
-// tile's position in memory. rs (32 entries per warp) is complete after the final __syncwarp.
+// The loads of one tile that do not depend on the gathered vector: this lane's local row
+// offset (lane i holds rp[i], i <= rows), and its run of column indices and values.
 template <class T>
-__device__ __forceinline__ void tile_row_sums(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
-                                              const T* __restrict__ val, const T* __restrict__ xg, const Tile& t,
-                                              T* rs) {
-  const unsigned full = 0xffffffffu;
+struct TileLoad {
+  int rpl;
+  int c[kTileEMax];
+  T v[kTileEMax];
+};
+
+// Issues the loads of tile t (none is used here, so all are in flight together).
+template <class T>
+__device__ __forceinline__ void tile_load(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                                          const T* __restrict__ val, const Tile& t, TileLoad<T>& L) {
+  if (t.e_log2 < 0) return;  // a long row: streamed by long_row_sum / cta_row_sum
   const int lane = threadIdx.x & 31;
   const int E = 1 << t.e_log2;
   const int kb = lane << t.e_log2;
   const int ke = min(t.nnz, kb + E);
-  int rpl = t.nnz;  // lane i: local offset of row i (i <= rows), clamped to the tile
-  if (lane <= t.rows) {
-    const int v = row_ptr[t.row_begin + lane] - t.nnz_begin;
-    rpl = v < 0 ? 0 : (v > t.nnz ? t.nnz : v);
-  }
-  T vv[kTileEMax], xv[kTileEMax];
-  {
-    int c[kTileEMax];
+  L.rpl = lane <= t.rows ? row_ptr[t.row_begin + lane] : 0;
 #pragma unroll
-    for (int j = 0; j < kTileEMax; ++j) {
-      const bool in = j < E && kb + j < ke;
-      c[j] = in ? lds(col + t.nnz_begin + kb + j) : 0;
-      vv[j] = in ? lds(val + t.nnz_begin + kb + j) : T(0);
+  for (int j = 0; j < kTileEMax; ++j) {
+    const bool in = j < E && kb + j < ke;
+    L.c[j] = in ? lds(col + t.nnz_begin + kb + j) : 0;
+    L.v[j] = in ? lds(val + t.nnz_begin + kb + j) : T(0);
+  }
+}
+
+// Row sums of tile t from its loads: rs[r] = sum of val * xg[col] over row t.row_begin + r,
+// r < t.rows (a long-row tile, e_log2 < 0, goes to long_row_sum). Lane l owns the tile's nonzeros [l E, (l + 1) E), E = 2^e_log2: it gathers
+// their entries of xg (all in flight together) and sums them per row with one FMA per
+// nonzero. The row offsets are read from the lanes' registers with shuffles; a row that
+// crosses lanes is completed by a segmented shuffle scan of the lanes' trailing partial
+// sums. Every sum's order depends only on the tile, never on its position in memory. rs
+// (32 entries per warp) is complete after the final __syncwarp.
+// One row of up to kLongNnz nonzeros summed by the whole warp: rounds of 32 x kLongRound
+// coalesced (column, value) loads, all issued before the round's gathers, FMAs into four
+// independent accumulators per lane, then a fixed-order tree.
+template <class T>
+__device__ __forceinline__ T long_row_sum(const int32_t* __restrict__ col, const T* __restrict__ val,
+                                          const T* __restrict__ xg, const Tile& t) {
+  const int lane = threadIdx.x & 31;
+  T acc[4] = {T(0), T(0), T(0), T(0)};
+  const int32_t* cp = col + t.nnz_begin;
+  const T* vp = val + t.nnz_begin;
+  for (int r0 = 0; r0 < t.nnz; r0 += 32 * kLongRound) {
+    int c[kLongRound];
+    T v[kLongRound];
+#pragma unroll
+    for (int j = 0; j < kLongRound; ++j) {
+      const int k = r0 + j * 32 + lane;
+      c[j] = k < t.nnz ? lds(cp + k) : 0;
+      v[j] = k < t.nnz ? lds(vp + k) : T(0);
     }
 #pragma unroll
-    for (int j = 0; j < kTileEMax; ++j) xv[j] = (j < E && kb + j < ke) ? xg[c[j]] : T(0);
+    for (int j = 0; j < kLongRound; ++j)
+      if (r0 + j * 32 + lane < t.nnz) acc[j & 3] = fma(v[j], xg[c[j]], acc[j & 3]);
   }
+  return warp_sum((acc[0] + acc[1]) + (acc[2] + acc[3]));  // valid in lane 0
+}
+
+// One row (or piece) of a CTA tile summed by all 8 warps: warp w takes rounds w, w + 8, ...
+// of 32 x kLongRound coalesced nonzeros, then the warps' sums are added in warp order.
+// Every thread must call it; the sum is written to *out, valid after the final barrier.
+template <class T>
+__device__ __forceinline__ void cta_row_sum(const int32_t* __restrict__ col, const T* __restrict__ val,
+                                            const T* __restrict__ xg, const Tile& t, T* wpart, T* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T acc[4] = {T(0), T(0), T(0), T(0)};
+  const int32_t* cp = col + t.nnz_begin;
+  const T* vp = val + t.nnz_begin;
+  for (int r0 = warp * 32 * kLongRound; r0 < t.nnz; r0 += kBlock * kLongRound) {
+    int c[kLongRound];
+    T v[kLongRound];
+#pragma unroll
+    for (int j = 0; j < kLongRound; ++j) {
+      const int k = r0 + j * 32 + lane;
+      c[j] = k < t.nnz ? lds(cp + k) : 0;
+      v[j] = k < t.nnz ? lds(vp + k) : T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < kLongRound; ++j)
+      if (r0 + j * 32 + lane < t.nnz) acc[j & 3] = fma(v[j], xg[c[j]], acc[j & 3]);
+  }
+  const T ws = warp_sum((acc[0] + acc[1]) + (acc[2] + acc[3]));
+  if (lane == 0) wpart[warp] = ws;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T s = T(0);
+    for (int w = 0; w < kBlock / 32; ++w) s += wpart[w];
+    *out = s;
+  }
+  __syncthreads();
+}
+
+template <class T>
+__device__ __forceinline__ void tile_sums(const int32_t* __restrict__ col, const T* __restrict__ val,
+                                          const T* __restrict__ xg, const Tile& t, const TileLoad<T>& L, T* rs) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  if (t.e_log2 < 0) {
+    const T sum = long_row_sum(col, val, xg, t);
+    if (lane == 0) rs[0] = sum;
+    __syncwarp();
+    return;
+  }
+  const int E = 1 << t.e_log2;
+  const int kb = lane << t.e_log2;
+  const int ke = min(t.nnz, kb + E);
+  int rpl = t.nnz;  // local offset of row `lane`, clamped to the tile
+  if (lane <= t.rows) {
+    const int v = L.rpl - t.nnz_begin;
+    rpl = v < 0 ? 0 : (v > t.nnz ? t.nnz : v);
+  }
+  T xv[kTileEMax];
+#pragma unroll
+  for (int j = 0; j < kTileEMax; ++j) xv[j] = (j < E && kb + j < ke) ? xg[L.c[j]] : T(0);
   // first row whose end lies beyond kb (lane 0 starts at row 0: leading empty rows are its)
   int r;
   {
@@ -78,7 +160,7 @@ __device__ __forceinline__ void tile_row_sums(const int32_t* __restrict__ row_pt
       }
       next = __shfl_sync(full, rpl, min(r + 1, 31));
     }
-    if (in) s = fma(vv[j], xv[j], s);
+    if (in) s = fma(L.v[j], xv[j], s);
   }
   while (true) {
     const bool need = active && r < t.rows && next <= ke;
@@ -115,6 +197,18 @@ __device__ __forceinline__ void tile_row_sums(const int32_t* __restrict__ row_pt
     if (head_row >= 0) rs[head_row] = head_sum + prev;
   }
   __syncwarp();
+}
+
+// A CTA's tile descriptors, staged in shared memory once (one coalesced copy) so that no
+// warp waits on a descriptor load before issuing a tile's loads.
+__device__ __forceinline__ int stage_tiles(const Tile* __restrict__ tiles, int tb, int te, Tile* tl) {
+  const int nt = te - tb;
+  const int* src = reinterpret_cast<const int*>(tiles + tb);
+  int* dst = reinterpret_cast<int*>(tl);
+  constexpr int kWords = (int)(sizeof(Tile) / sizeof(int));
+  for (int i = threadIdx.x; i < nt * kWords; i += kBlock) dst[i] = src[i];
+  __syncthreads();
+  return nt;
 }
 
 // A piece of a split row: its partial goes to the row's carry slot, and the warp whose

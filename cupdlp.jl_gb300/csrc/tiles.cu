@@ -40,13 +40,24 @@ void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t
   while (r < r1) {
     const long long lr = len(r);
     if (lr > kTileNnz) {
-      const int32_t pieces = (int32_t)((lr + kTileNnz - 1) / kTileNnz);
-      const int32_t sid = splits++;
-      const int32_t cb = carries;
-      carries += pieces;
-      for (int32_t q = 0; q < pieces; ++q)
-        push(r, 1, (long long)rp[r] + (long long)q * kTileNnz,
-             std::min<long long>(kTileNnz, lr - (long long)q * kTileNnz), sid, q, pieces, cb);
+      if (lr <= kLongNnz) {
+        push(r, 1, rp[r], lr, -1, 0, 1, 0);
+        out.back().e_log2 = kWarpLong;
+        ++r;
+        continue;
+      }
+      const int32_t pieces = (int32_t)((lr + kCtaNnz - 1) / kCtaNnz);
+      int32_t sid = -1, cb = 0;
+      if (pieces > 1) {
+        sid = splits++;
+        cb = carries;
+        carries += pieces;
+      }
+      for (int32_t q = 0; q < pieces; ++q) {
+        push(r, 1, (long long)rp[r] + (long long)q * kCtaNnz,
+             std::min<long long>(kCtaNnz, lr - (long long)q * kCtaNnz), sid, q, pieces, cb);
+        out.back().e_log2 = kCtaLong;
+      }
       ++r;
       continue;
     }
@@ -74,14 +85,20 @@ void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector
     inst_split[k] = splits;
     const size_t t0 = tiles.size();
     list_tiles(M.host_rp.data(), bounds[k], bounds[k + 1], k, aux.empty() ? 0 : aux[k], tiles, splits, carries);
-    // CTAs: consecutive tiles of this instance, as even as possible; tiles per CTA grow
-    // from 8 to 32 once the instance has more than ~1,200 tiles (8 CTAs per SM of 152)
+    // CTAs: a CTA tile alone; other consecutive tiles of this instance in groups of tpc,
+    // where tpc grows from 8 to 32 once the instance has more than ~1,200 tiles (8 CTAs
+    // per SM of 152)
     const long long nt = (long long)(tiles.size() - t0);
     const long long tpc = std::min<long long>(kTilesPerCtaMax, std::max<long long>(kTilesPerCtaMin, (nt + 1215) / 1216));
-    const long long nc = (nt + tpc - 1) / tpc;
-    for (long long c = 0; c < nc; ++c) {
-      cta_begin.push_back((int32_t)(t0 + (nt * c) / nc));
-      cta_inst.push_back(k);
+    long long open = 0;  // tiles in the CTA being filled
+    for (size_t q = t0; q < tiles.size(); ++q) {
+      const bool cta_tile = tiles[q].e_log2 == kCtaLong;
+      if (cta_tile || open == 0 || open == tpc) {
+        cta_begin.push_back((int32_t)q);
+        cta_inst.push_back(k);
+        open = 0;
+      }
+      open = cta_tile ? tpc : open + 1;  // nothing joins a CTA tile
     }
   }
   inst_cta[K] = (int32_t)cta_inst.size();

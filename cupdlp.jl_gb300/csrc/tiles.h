@@ -1,8 +1,10 @@
 // tiles.h — the work decomposition of the step kernels: warp tiles grouped into CTAs.
 //
 // A tile is one warp's share of a CSR matrix: consecutive rows holding at most kTileNnz
-// nonzeros and at most kTileRows rows; a row longer than kTileNnz is cut into pieces of
-// kTileNnz, one tile each, whose partial sums meet in a carry array. Consecutive tiles of
+// nonzeros and at most kTileRows rows, or one row of up to kLongNnz nonzeros streamed by
+// the warp in rounds. A longer row is a CTA tile: a CTA of its own whose 8 warps split
+// the row and combine their sums in shared memory; a row longer than kCtaNnz is cut into
+// CTA pieces of kCtaNnz whose partial sums meet in a carry array. Consecutive tiles of
 // one instance form a CTA's work (8 to 32 tiles, dealt to its 8 warps in turn), so
 // every CTA belongs to exactly one instance and the per-instance step decision can count
 // CTAs. An instance with few tiles gets one tile per warp (most CTAs in flight), a large one
@@ -19,15 +21,22 @@ namespace gpdhg {
 constexpr int kTileNnz = 256;     // nonzeros per tile (32 lanes x at most 8)
 constexpr int kTileRows = 31;     // rows per tile: rows + 1 row offsets fit in 32 lanes
 constexpr int kTileEMax = 8;      // nonzeros per lane
+constexpr int kLongNnz = 1024;    // longest row one warp streams alone
+constexpr int kCtaNnz = 16384;    // longest row (piece) one CTA sums
+constexpr int kLongRound = 8;     // (column, value) loads per lane and round of a long row
 constexpr int kTilesPerCtaMin = 8;   // tiles per CTA: one per warp for small instances,
 constexpr int kTilesPerCtaMax = 32;  // up to four per warp for large ones
+
+constexpr int kWarpLong = -1;
+constexpr int kCtaLong = -2;
 
 struct Tile {
   int32_t row_begin;  // first row (packed numbering)
   int32_t rows;       // rows of the tile (1 for a piece of a split row, 0 for an empty instance)
   int32_t nnz_begin;  // first nonzero in the CSR
   int32_t nnz;        // nonzeros of the tile
-  int32_t e_log2;     // log2 of the nonzeros per lane
+  int32_t e_log2;     // log2 of the nonzeros per lane; kWarpLong: one row streamed by the
+                      // warp; kCtaLong: one row (or piece) summed by a whole CTA
   int32_t split;      // -1, or the split row this piece belongs to
   int32_t piece;      // piece index within the split row
   int32_t pieces;     // pieces of the split row
