@@ -44,7 +44,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="transportation",
-                    choices=["transportation", "plain", "powerlaw", "batch"])
+                    choices=["transportation", "plain", "powerlaw", "batch", "serve"])
+    ap.add_argument("--serve-rates", default="50,200,1000", help="Poisson arrival rates (LPs/s)")
+    ap.add_argument("--serve-duration", type=float, default=5.0, help="seconds of arrivals per rate")
+    ap.add_argument("--serve-drain-cap", type=float, default=90.0,
+                    help="seconds after the last arrival before unfinished requests are counted as such")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--tolerance", type=float, default=1e-4)
     ap.add_argument("--cpu-sample-iters", type=int, default=0, help="oracle iteration cap (0: automatic)")
@@ -303,7 +307,134 @@ def run_batch(args):
     return 0
 
 
+def run_serve(args):
+    """Continuous batching (gpdhg_server_*) under Poisson arrivals: 70% small LPs (m 200-2,000),
+    25% medium (m 10k-100k), 5% large (power-law m = 500k, nnz = 10M), drawn from a seeded pool
+    of pre-generated, pre-scaled instances; small and medium in FP64, large in FP32, tolerance
+    1e-4. Latency = result available on the host - arrival; value = completed requests / s at the
+    middle rate. Beside it, the plain per-request form on the same GPU: one gpdhg_problem at a
+    time in arrival order, its latencies from the queue driven by each pool LP's measured
+    create + solve + copy-back time."""
+    world, rank, local, pg = dist_setup(args.gpus)
+    import threading
+    import torch
+    import cupdlp
+    from cupdlp import synthetic
+    from cupdlp.solver import DeviceProblem, Server, scaled_desc
+    torch.cuda.set_device(local)
+    torch.zeros(1, device="cuda")
+    rng = np.random.default_rng(7 + rank)
+    pool = {"small": [], "medium": [], "large": []}
+    sizes = {"small": 16, "medium": 4, "large": 1}
+    for kind, cnt in sizes.items():
+        for _ in range(cnt):
+            lp = synthetic.serving_mixture_lp(rng, kind)
+            sq = cupdlp.rescale_problem(10, False, 1.0, 0, lp.problem)
+            pool[kind].append(scaled_desc(sq))
+    p64 = cupdlp.default_parameters(tolerance=1e-4, precision=cupdlp.Precision.FP64, record_iteration_stats=False,
+                                    iteration_limit=20_000, time_sec_limit=120.0)
+    p32 = cupdlp.default_parameters(tolerance=1e-4, precision=cupdlp.Precision.FP32, record_iteration_stats=False,
+                                    iteration_limit=1_000, time_sec_limit=120.0)
+    par = {"small": p64, "medium": p64, "large": p32}
+    # measured service time of every pool LP alone (create + solve + copy back), after a warm-up
+    service = {}
+    for kind, descs in pool.items():
+        for i, d in enumerate(descs):
+            for rep in range(2):
+                t0 = time.perf_counter()
+                with DeviceProblem(d) as dp:
+                    dp.solve(par[kind], want_solution=True)
+                service[(kind, i)] = time.perf_counter() - t0
+    rates = [float(r) for r in args.serve_rates.split(",")]
+    mix = (0.70, 0.25, 0.05)
+    per_rate = {}
+    launches = 0
+    with ClockSampler(local) as clk:
+        for rate in rates:
+            arr = []
+            t = 0.0
+            while True:
+                t += rng.exponential(1.0 / rate)
+                if t > args.serve_duration:
+                    break
+                u = rng.random()
+                kind = "small" if u < mix[0] else ("medium" if u < mix[0] + mix[1] else "large")
+                arr.append((t, kind, int(rng.integers(0, len(pool[kind])))))
+            done = {}
+            lock = threading.Lock()
+            with Server(hbm_budget_bytes=150e9, workers=3, max_cohort=256, linger_sec=0.002) as srv:
+                tickets = {}
+                stop = threading.Event()
+
+                def collect():
+                    while not stop.is_set() or len(done) < len(tickets):
+                        with lock:
+                            pending = [(tk, q) for q, tk in tickets.items() if q not in done]
+                        for tk, q in pending:
+                            if srv.poll(tk) is not None:
+                                done[q] = time.perf_counter()
+                        if stop.is_set() and time.perf_counter() > deadline:
+                            return
+                        time.sleep(0.0005)
+
+                deadline = float("inf")
+                col = threading.Thread(target=collect, daemon=True)
+                col.start()
+                t_start = time.perf_counter()
+                for q, (ta, kind, i) in enumerate(arr):
+                    now = time.perf_counter() - t_start
+                    if ta > now:
+                        time.sleep(ta - now)
+                    tk = srv.submit(pool[kind][i], par[kind])
+                    with lock:
+                        tickets[q] = tk
+                deadline = time.perf_counter() + args.serve_drain_cap
+                stop.set()
+                col.join()
+            lat = sorted(done[q] - (t_start + arr[q][0]) for q in done)
+            span = (max(done.values()) - t_start) if done else float("nan")
+            # the plain per-request form: one LP at a time in arrival order
+            free_at, seq_lat = 0.0, []
+            for (ta, kind, i) in arr:
+                start = max(ta, free_at)
+                free_at = start + service[(kind, i)]
+                seq_lat.append(free_at - ta)
+            seq_lat.sort()
+            pct = lambda v, p: v[min(len(v) - 1, int(p * len(v)))] if v else None
+            per_rate[str(int(rate))] = {
+                "requests": len(arr), "completed": len(done), "unfinished": len(arr) - len(done),
+                "solves_per_sec": len(done) / span if done else 0.0,
+                "p50_latency_sec": pct(lat, 0.50), "p99_latency_sec": pct(lat, 0.99),
+                "plain_per_request": {"solves_per_sec": len(arr) / free_at if free_at else None,
+                                      "p50_latency_sec": pct(seq_lat, 0.50), "p99_latency_sec": pct(seq_lat, 0.99)},
+                "mix": {k: sum(1 for a in arr if a[1] == k) for k in pool},
+            }
+    clocks = clk.summary()
+    mid = per_rate[str(int(rates[len(rates) // 2]))]
+    line = {
+        "metric": "served solves/sec (p50/p99 latency in config)", "value": mid["solves_per_sec"], "unit": "solves/s",
+        "n_gpus": world, "steps": len(rates), "warmup": 1, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 (small, medium) / f32+f64 (large)",
+        "data": "synthetic (seeded), Poisson arrivals",
+        "config": {"workload": "serving stream: 70% small (m 200-2,000), 25% medium (m 10k-100k), 5% large "
+                               "(power-law m 500k, nnz 10M); pool 16/4/1 pre-scaled instances; FP64 tol 1e-4 "
+                               "(large: FP32, 1,000-iteration cap)",
+                   "duration_sec_per_rate": args.serve_duration, "hbm_budget_bytes": 150e9, "workers": 3,
+                   "rates": per_rate,
+                   "service_sec_alone": {f"{k}[{i}]": v for (k, i), v in service.items()}},
+        "e2e": {"value": mid["solves_per_sec"], "unit": "solves/s", "note": "host LP in, host solution out"},
+        "gpu_launches": None, "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
 def run_ours(args):
+    if args.workload == "serve":
+        return run_serve(args)
     if args.workload == "batch":
         return run_batch(args)
     world, rank, local, pg = dist_setup(args.gpus)

@@ -213,6 +213,63 @@ gpdhg_status gpdhg_convergence_noalloc(int32_t num_variables, int32_t num_constr
   });
 }
 
+double gpdhg_server_footprint(const gpdhg_lp_desc* desc, const gpdhg_params* params) {
+  if (!desc || !params) return -1.0;
+  return gpdhg::footprint_bytes(*desc, *params);
+}
+
+gpdhg_status gpdhg_server_create(const gpdhg_server_config* cfg, gpdhg_server** out) {
+  return guarded([&] {
+    if (!out) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    gpdhg_server_config c{};
+    if (cfg) c = *cfg;
+    *out = gpdhg::server_create(c);
+  });
+}
+
+gpdhg_status gpdhg_server_submit(gpdhg_server* s, const gpdhg_lp_desc* desc, const gpdhg_params* params,
+                                 uint64_t* ticket) {
+  return guarded([&] {
+    if (!s || !desc || !ticket) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "server, desc or ticket is NULL");
+    check_params(params);
+    if (params->precision == GPDHG_PRECISION_FP32_REFINE)
+      throw gpdhg::Error(GPDHG_ERR_NOT_SUPPORTED, "served solves run in FP64 or FP32 (no FP64 hand-off)");
+    if (params->step_size_policy != GPDHG_STEPSIZE_ADAPTIVE)
+      throw gpdhg::Error(GPDHG_ERR_NOT_SUPPORTED, "served solves use the adaptive step size");
+    *ticket = gpdhg::server_submit(s, *desc, *params);
+  });
+}
+
+namespace {
+gpdhg_status server_take(gpdhg_server* s, uint64_t ticket, double timeout_sec, gpdhg_result* result,
+                         double* primal_out, double* dual_out) {
+  gpdhg_status st = GPDHG_OK;
+  const gpdhg_status g = guarded([&] {
+    if (!s) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "server is NULL");
+    std::string err;
+    st = gpdhg::server_take(s, ticket, timeout_sec, result, primal_out, dual_out, err);
+    if (st == GPDHG_ERR_NOT_READY) err = "request has not terminated yet";
+    if (st != GPDHG_OK) throw gpdhg::Error(st, err);
+  });
+  return g;
+}
+}  // namespace
+
+gpdhg_status gpdhg_server_poll(gpdhg_server* s, uint64_t ticket, gpdhg_result* result, double* primal_out,
+                               double* dual_out) {
+  return server_take(s, ticket, 0.0, result, primal_out, dual_out);
+}
+
+gpdhg_status gpdhg_server_wait(gpdhg_server* s, uint64_t ticket, double timeout_sec, gpdhg_result* result,
+                               double* primal_out, double* dual_out) {
+  return server_take(s, ticket, timeout_sec > 0.0 ? timeout_sec : 0.0, result, primal_out, dual_out);
+}
+
+gpdhg_status gpdhg_server_destroy(gpdhg_server* s) {
+  return guarded([&] { gpdhg::server_destroy(s); });
+}
+
 gpdhg_status gpdhg_batch_destroy(gpdhg_batch* b) {
   return guarded([&] { delete b; });
 }

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "host_logic.h"
@@ -47,4 +48,13 @@ namespace gpdhg {
 void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs);
 void batch_solve(gpdhg_batch* B, const gpdhg_params& prm, gpdhg_result* results, double* const* primal_out,
                  double* const* dual_out);
+
+// Serving loop (server.cu).
+double footprint_bytes(const gpdhg_lp_desc& d, const gpdhg_params& p);
+gpdhg_server* server_create(const gpdhg_server_config& cfg);
+void server_destroy(gpdhg_server* s);
+uint64_t server_submit(gpdhg_server* s, const gpdhg_lp_desc& d, const gpdhg_params& p);
+// OK (outputs copied, ticket released), NOT_READY, or the request's error (err set).
+gpdhg_status server_take(gpdhg_server* s, uint64_t ticket, double timeout_sec, gpdhg_result* r, double* x,
+                         double* y, std::string& err);
 }  // namespace gpdhg

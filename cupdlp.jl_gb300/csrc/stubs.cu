@@ -7,16 +7,4 @@ gpdhg_status gpdhg_problem_create_unscaled(const gpdhg_lp_desc*, const gpdhg_par
   return GPDHG_ERR_NOT_SUPPORTED;
 }
 gpdhg_status gpdhg_get_rescaling(const gpdhg_problem*, double*, double*) { return GPDHG_ERR_NOT_SUPPORTED; }
-gpdhg_status gpdhg_server_create(const gpdhg_server_config*, gpdhg_server** out) {
-  if (out) *out = nullptr;
-  return GPDHG_ERR_NOT_SUPPORTED;
-}
-gpdhg_status gpdhg_server_submit(gpdhg_server*, const gpdhg_lp_desc*, const gpdhg_params*, uint64_t*) {
-  return GPDHG_ERR_NOT_SUPPORTED;
-}
-gpdhg_status gpdhg_server_poll(gpdhg_server*, uint64_t, gpdhg_result*, double*, double*) { return GPDHG_ERR_NOT_SUPPORTED; }
-gpdhg_status gpdhg_server_wait(gpdhg_server*, uint64_t, double, gpdhg_result*, double*, double*) {
-  return GPDHG_ERR_NOT_SUPPORTED;
-}
-gpdhg_status gpdhg_server_destroy(gpdhg_server*) { return GPDHG_ERR_NOT_SUPPORTED; }
 }

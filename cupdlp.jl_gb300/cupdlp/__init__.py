@@ -14,7 +14,8 @@ from .types import (AdaptiveStepsizeParams, ConstantStepsizeParams, ConvergenceI
                     params_to_c, termination_reason_to_string, validate_termination_criteria)
 from .preprocess import (InvalidProblemError, l2_norm_rescaling, pock_chambolle_rescaling,  # noqa: F401
                          rescale_problem, ruiz_rescaling, scale_problem, unscale_problem, validate)
-from .solver import DeviceBatch, DeviceProblem, optimize, optimize_batch, scaled_desc, unscaled_desc  # noqa: F401
+from .solver import (DeviceBatch, DeviceProblem, Server, optimize, optimize_batch, scaled_desc,  # noqa: F401
+                     unscaled_desc)
 from . import _abi  # noqa: F401
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -161,8 +161,11 @@ class ServerConfig(C.Structure):
     _fields_ = [
         ("hbm_budget_bytes", C.c_double),
         ("max_resident", C.c_int32),
-        ("steps_per_round", C.c_int32),
-        ("reserved", C.c_double * 4),
+        ("max_cohort", C.c_int32),
+        ("workers", C.c_int32),
+        ("reserved_int", C.c_int32),
+        ("linger_sec", C.c_double),
+        ("reserved", C.c_double * 2),
     ]
 
 
@@ -187,6 +190,7 @@ SIGNATURES = {
     "gpdhg_batch_destroy": (C.c_int, [C.c_void_p]),
     "gpdhg_convergence_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_double] + [_dp] * 8
                                   + [C.c_double, C.c_double, C.c_void_p, C.POINTER(ConvergenceInformation)]),
+    "gpdhg_server_footprint": (C.c_double, [C.POINTER(LpDesc), C.POINTER(Params)]),
     "gpdhg_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
     "gpdhg_server_submit": (C.c_int, [C.c_void_p, C.POINTER(LpDesc), C.POINTER(Params),
                                       C.POINTER(C.c_uint64)]),

@@ -250,3 +250,78 @@ def optimize_batch(params: PdhgParameters, problems) -> List[SaddlePointOutput]:
                                      termination_reason_to_string(reason), int(r.iteration_count),
                                      [stats_from_c(r.last_iteration_stats)], r))
     return out
+
+
+class Server:
+    """A gpdhg_server: continuous batching of arriving scaled LPs on the GPU.
+
+    submit() copies the LP and returns a ticket at once; poll() / wait() hand back
+    (result, x, y) once the request has terminated (each ticket once). Requests are packed
+    into device batches by worker threads as memory and workers free up, so results are
+    bit-identical to solving each LP alone with the same parameters."""
+
+    def __init__(self, hbm_budget_bytes: float = 0.0, max_resident: int = 0, max_cohort: int = 0,
+                 workers: int = 0, linger_sec: float = 0.0, lib=None):
+        self.lib = lib or _abi.load()
+        cfg = _abi.ServerConfig()
+        cfg.hbm_budget_bytes = hbm_budget_bytes
+        cfg.max_resident = max_resident
+        cfg.max_cohort = max_cohort
+        cfg.workers = workers
+        cfg.linger_sec = linger_sec
+        h = C.c_void_p()
+        _abi.check(self.lib.gpdhg_server_create(C.byref(cfg), C.byref(h)), self.lib)
+        self.handle = h
+        self._shapes = {}
+
+    def footprint(self, desc: "_Desc", params: PdhgParameters) -> float:
+        cp = params_to_c(params)
+        return float(self.lib.gpdhg_server_footprint(desc.ref, C.byref(cp)))
+
+    def submit(self, desc: "_Desc", params: PdhgParameters) -> int:
+        cp = params_to_c(params)
+        t = C.c_uint64()
+        _abi.check(self.lib.gpdhg_server_submit(self.handle, desc.ref, C.byref(cp), C.byref(t)), self.lib)
+        self._shapes[t.value] = (desc.desc.num_variables, desc.desc.num_constraints)
+        return t.value
+
+    def _take(self, ticket: int, timeout: float | None):
+        n, m = self._shapes.get(ticket, (0, 0))   # unknown tickets are reported by the library
+        res = _abi.Result()
+        x = np.empty(n)
+        y = np.empty(max(m, 1))
+        if timeout is None:
+            st = self.lib.gpdhg_server_poll(self.handle, ticket, C.byref(res), _abi.dptr(x), _abi.dptr(y))
+        else:
+            st = self.lib.gpdhg_server_wait(self.handle, ticket, float(timeout), C.byref(res), _abi.dptr(x),
+                                            _abi.dptr(y))
+        if st == _abi.ERR_NOT_READY:
+            return None
+        self._shapes.pop(ticket, None)
+        _abi.check(st, self.lib)
+        return res, x, y[:m]
+
+    def poll(self, ticket: int):
+        """(result, x, y) if the request has terminated, else None."""
+        return self._take(ticket, None)
+
+    def wait(self, ticket: int, timeout: float = 3600.0):
+        """Blocks until the request terminates (None after `timeout` seconds)."""
+        return self._take(ticket, timeout)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.gpdhg_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

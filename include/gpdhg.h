@@ -342,24 +342,44 @@ gpdhg_status gpdhg_convergence_noalloc(int32_t num_variables, int32_t num_constr
                                        gpdhg_convergence_information* out);
 
 /* ---------------------------------------------------------------------------------
- * Serving loop: continuous batching of arriving LPs. Requests are admitted by HBM
- * footprint, packed into free slots of a device-resident batch, advanced together,
- * retired when they terminate and back-filled by waiting requests.
+ * Serving loop: continuous batching of arriving LPs (no reference counterpart: a request
+ * loop around optimize(), src/primal_dual_hybrid_gradient_gpu.jl:457).
+ *
+ * Requests wait in a FIFO queue. Each of `workers` host threads owns a CUDA stream and
+ * repeatedly packs the waiting requests that share the head request's parameters (at most
+ * max_cohort of them, after lingering up to linger_sec for more) into one device batch
+ * (gpdhg_batch_*, a segmented CSR with per-instance step size, restarts and termination)
+ * and solves it. A cohort is admitted only while the estimated device footprint of all
+ * resident requests stays within hbm_budget_bytes and at most max_resident requests are
+ * resident, so requests arriving while others run start as soon as memory and a worker
+ * are free, and their kernels overlap with the running cohorts' on the device. An instance
+ * that terminates stops launching work at once; its cohort's memory is released when the
+ * cohort's last instance terminates. Each result is bit-identical to solving the same LP
+ * alone with the same parameters (a batch gives every instance the same arithmetic as a
+ * lone solve). Zero config fields take the defaults in brackets.
  * ------------------------------------------------------------------------------- */
 typedef struct gpdhg_server gpdhg_server;
 
 typedef struct gpdhg_server_config {
-  double hbm_budget_bytes;   /* admission budget for resident requests */
-  int32_t max_resident;      /* slot count of the device batch */
-  int32_t steps_per_round;   /* PDHG iterations between admission rounds */
-  double reserved[4];
+  double hbm_budget_bytes;   /* admission budget for resident requests [half the free device memory] */
+  int32_t max_resident;      /* requests resident on the device at once, all cohorts [4096] */
+  int32_t max_cohort;        /* requests packed into one device batch [256] */
+  int32_t workers;           /* cohorts advanced concurrently [2] */
+  int32_t reserved_int;
+  double linger_sec;         /* a free worker waits this long for more requests [0.002] */
+  double reserved[2];
 } gpdhg_server_config;
 
+/* Estimated device bytes one request occupies while resident (the admission measure). */
+double gpdhg_server_footprint(const gpdhg_lp_desc* desc, const gpdhg_params* params);
 gpdhg_status gpdhg_server_create(const gpdhg_server_config* cfg, gpdhg_server** out);
-/* Copies the request; `ticket` identifies it. GPDHG_ERR_ADMISSION if it can never fit. */
+/* Copies the request; `ticket` identifies it. GPDHG_ERR_ADMISSION if it can never fit.
+ * The parameters must be batchable: FP64 or FP32 precision, adaptive step size. */
 gpdhg_status gpdhg_server_submit(gpdhg_server* s, const gpdhg_lp_desc* desc, const gpdhg_params* params,
                                  uint64_t* ticket);
-/* Non-blocking: GPDHG_ERR_NOT_READY until the request has terminated. */
+/* Non-blocking: GPDHG_ERR_NOT_READY until the request has terminated. A request's result
+ * is handed out once: after a successful poll or wait its ticket is released. primal_out
+ * and dual_out (n and m doubles, or NULL) receive the scaled average iterate. */
 gpdhg_status gpdhg_server_poll(gpdhg_server* s, uint64_t ticket, gpdhg_result* result,
                                double* primal_out, double* dual_out);
 /* Blocks until the request has terminated or `timeout_sec` passes (GPDHG_ERR_NOT_READY). */

@@ -9,7 +9,8 @@ import pytest
 
 import cupdlp
 from cupdlp import _abi
-from cupdlp.solver import unscaled_desc
+from cupdlp import synthetic
+from cupdlp.solver import scaled_desc, unscaled_desc
 
 import instances
 
@@ -95,3 +96,25 @@ def test_null_arguments(lib):
     st = _abi.IterationStats()
     assert lib.gpdhg_get_stats(None, 0, C.byref(st)) == _abi.ERR_INVALID_ARGUMENT
     assert "NULL" in lib.gpdhg_last_error().decode()
+
+
+def test_server_footprint_and_null_handling():
+    """Host-only parts of the serving API: the admission footprint grows with the LP and
+    the precision, and NULL handles are rejected without touching the GPU."""
+    lib = _abi.load()
+    small = synthetic.known_optimum_lp(0, m=100, n=200, density=0.05)
+    big = synthetic.known_optimum_lp(1, m=1000, n=2000, density=0.005)
+    ds = scaled_desc(cupdlp.rescale_problem(10, False, 1.0, 0, small.problem))
+    db = scaled_desc(cupdlp.rescale_problem(10, False, 1.0, 0, big.problem))
+    p64 = cupdlp.params_to_c(cupdlp.default_parameters(precision=cupdlp.Precision.FP64))
+    p32 = cupdlp.params_to_c(cupdlp.default_parameters(precision=cupdlp.Precision.FP32))
+    f_small = lib.gpdhg_server_footprint(ds.ref, C.byref(p64))
+    f_big = lib.gpdhg_server_footprint(db.ref, C.byref(p64))
+    assert 0 < f_small < f_big
+    assert lib.gpdhg_server_footprint(db.ref, C.byref(p32)) < f_big
+    assert lib.gpdhg_server_footprint(None, None) < 0
+    t = C.c_uint64()
+    assert lib.gpdhg_server_submit(None, ds.ref, C.byref(p64), C.byref(t)) == _abi.ERR_INVALID_ARGUMENT
+    assert lib.gpdhg_server_poll(None, 1, None, None, None) == _abi.ERR_INVALID_ARGUMENT
+    assert lib.gpdhg_server_wait(None, 1, 0.0, None, None, None) == _abi.ERR_INVALID_ARGUMENT
+    assert lib.gpdhg_server_create(None, None) == _abi.ERR_INVALID_ARGUMENT

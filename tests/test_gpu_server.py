@@ -1,0 +1,96 @@
+"""GPU tests of the serving loop (gpdhg_server_*): requests that arrive while others are
+on the device are admitted as workers and memory free up, and every result is the same,
+bit for bit, as the same LP solved alone with the same parameters."""
+import time
+
+import numpy as np
+import pytest
+
+import cupdlp
+from cupdlp import synthetic
+from cupdlp.solver import DeviceProblem, Server, scaled_desc
+
+pytestmark = pytest.mark.gpu
+
+
+def _params(precision, tol):
+    # the iteration limit keeps every request's end independent of the wall clock
+    return cupdlp.default_parameters(tolerance=tol, precision=precision, iteration_limit=60_000,
+                                     time_sec_limit=300.0)
+
+
+def _stream(seed, count):
+    lps = synthetic.batch_lps(seed, count=count, median_m=300, m_range=(60, 2500))
+    return [cupdlp.rescale_problem(10, False, 1.0, 0, lp.problem) for lp in lps]
+
+
+def _alone(sq, params):
+    with DeviceProblem(scaled_desc(sq)) as dp:
+        return dp.solve(params)
+
+
+def _same(served, alone, k):
+    (rs, xs, ys), (ra, xa, ya) = served, alone
+    assert rs.termination_reason == ra.termination_reason, k
+    assert rs.iteration_count == ra.iteration_count, k
+    assert rs.total_number_iterations == ra.total_number_iterations, k
+    assert np.array_equal(xs, xa), k
+    assert np.array_equal(ys, ya), k
+    cs = rs.last_iteration_stats.convergence_information
+    ca = ra.last_iteration_stats.convergence_information
+    assert cs.primal_objective == ca.primal_objective and cs.dual_objective == ca.dual_objective, k
+
+
+@pytest.mark.parametrize("precision,tol", [(cupdlp.Precision.FP64, 1e-6), (cupdlp.Precision.FP32, 1e-4)])
+def test_served_equals_alone_in_a_mix(precision, tol):
+    scaled = _stream(31, 12)
+    params = _params(precision, tol)
+    descs = [scaled_desc(sq) for sq in scaled]
+    with Server(workers=2, max_cohort=4, linger_sec=0.001) as srv:
+        tickets = []
+        # three waves: later requests arrive while earlier cohorts are on the GPU
+        for wave in range(3):
+            for d in descs[4 * wave:4 * wave + 4]:
+                tickets.append(srv.submit(d, params))
+            time.sleep(0.05)
+        served = [srv.wait(t, timeout=600.0) for t in tickets]
+    for k, sq in enumerate(scaled):
+        assert served[k] is not None, k
+        _same(served[k], _alone(sq, params), k)
+
+
+def test_backfill_under_a_tight_budget_and_mixed_parameters():
+    scaled = _stream(32, 8)
+    p_a = _params(cupdlp.Precision.FP64, 1e-4)
+    p_b = _params(cupdlp.Precision.FP64, 1e-6)
+    descs = [scaled_desc(sq) for sq in scaled]
+    with Server(workers=2, max_cohort=3) as srv:
+        biggest = max(srv.footprint(d, p_a) for d in descs)
+    # room for about two of the largest requests at a time: the rest wait and back-fill
+    with Server(hbm_budget_bytes=2.2 * biggest, workers=2, max_cohort=3) as srv:
+        plist = [p_a if k % 2 == 0 else p_b for k in range(len(descs))]
+        tickets = [srv.submit(d, p) for d, p in zip(descs, plist)]
+        served = [srv.wait(t, timeout=600.0) for t in tickets]
+    for k, (sq, p) in enumerate(zip(scaled, plist)):
+        _same(served[k], _alone(sq, p), k)
+
+
+def test_admission_and_ticket_lifecycle():
+    sq = _stream(33, 1)[0]
+    d = scaled_desc(sq)
+    params = _params(cupdlp.Precision.FP64, 1e-6)
+    with Server(hbm_budget_bytes=1e5, workers=1) as srv:
+        with pytest.raises(cupdlp._abi.GpdhgError) as e:
+            srv.submit(d, params)
+        assert e.value.status == cupdlp._abi.ERR_ADMISSION
+    with Server(workers=1) as srv:
+        t = srv.submit(d, params)
+        got = srv.wait(t, timeout=600.0)
+        assert got is not None and got[0].termination_reason == 1
+        with pytest.raises(cupdlp._abi.GpdhgError) as e:   # a ticket is handed out once
+            srv.wait(t, timeout=1.0)
+        assert e.value.status == cupdlp._abi.ERR_INVALID_ARGUMENT
+        # FP32_REFINE cannot be served (no hand-off inside a batch)
+        with pytest.raises(cupdlp._abi.GpdhgError) as e:
+            srv.submit(d, _params(cupdlp.Precision.FP32_REFINE, 1e-6))
+        assert e.value.status == cupdlp._abi.ERR_NOT_SUPPORTED
