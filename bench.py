@@ -186,6 +186,30 @@ def sum_over_ranks(pg, v):
     return float(t.item())
 
 
+PROFILE_FILES = {"transportation": "step_kernels_transportation_fp64.md", "powerlaw": "step_kernels_powerlaw_fp32.md"}
+
+
+def profile_traffic(workload_name, kernel):
+    """DRAM bytes per launch (read + write) of `kernel` in the committed ncu capture of this
+    workload (profiles/), averaged over the captured launches; None if there is none."""
+    fn = PROFILE_FILES.get(workload_name)
+    if not fn:
+        return None
+    try:
+        text = open(os.path.join(REPO, "profiles", fn)).read()
+    except OSError:
+        return None
+    vals = []
+    for line in text.splitlines():
+        cells = [c.strip() for c in line.strip().strip("|").split("|")]
+        if len(cells) > 3 and cells[0].startswith(kernel + "<"):
+            try:
+                vals.append((float(cells[2]) + float(cells[3])) * 1e6)
+            except ValueError:
+                pass
+    return sum(vals) / len(vals) if vals else None
+
+
 def cpu_baseline(lp_problem, params, iters_cap, threads=None):
     """The oracle on a bounded sample: the first `iters_cap` iterations of the same solve."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
@@ -507,8 +531,11 @@ def run_ours(args):
     dom = "primal_step_kernel" if tp >= td else "dual_step_kernel"
     b_dom, t_dom = (bytes_p, tp) if tp >= td else (bytes_d, td)
     achieved = (b_dom / t_dom / 1e9) if t_dom > 0 else None
+    traffic = profile_traffic(args.workload, dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": (achieved / peak) if achieved else None, "traffic": None,
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum, cold cache; "
+                                "profiles/" + PROFILE_FILES.get(args.workload, "-") + ")",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
                 "share_of_step_time": {"primal_step_kernel": tp / max(tp + td, 1e-30),
                                        "dual_step_kernel": td / max(tp + td, 1e-30)},
