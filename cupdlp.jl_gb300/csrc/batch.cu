@@ -278,8 +278,8 @@ struct BatchWorkspace {
                        part_p.get(), part_p_split.get(), part_d.get(), part_d_split.get(), mode, direct};
   }
   void launch_pair(int mode, cudaStream_t s) {
-    primal_step_kernel<T><<<plan_p.num_ctas, kBlock, 0, s>>>(pargs(mode));
-    dual_step_kernel<T><<<plan_d.num_ctas, kBlock, 0, s>>>(dargs(mode));
+    launch_step(primal_step_kernel<T>, plan_p.num_ctas, s, pargs(mode));
+    launch_step(dual_step_kernel<T>, plan_d.num_ctas, s, dargs(mode));
     launches += 2;
   }
   void launch_pair(int mode) { launch_pair(mode, B->stream); }
@@ -288,8 +288,8 @@ struct BatchWorkspace {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < pairs; ++k) {
-      primal_step_kernel<T><<<plan_p.num_ctas, kBlock, 0, s>>>(pargs(kStepNormal));
-      dual_step_kernel<T><<<plan_d.num_ctas, kBlock, 0, s>>>(dargs(kStepNormal));
+      launch_step(primal_step_kernel<T>, plan_p.num_ctas, s, pargs(kStepNormal));
+      launch_step(dual_step_kernel<T>, plan_d.num_ctas, s, dargs(kStepNormal));
     }
     cudaMemcpyAsync(st_host.p, st_dev.get(), sizeof(StepState) * count, cudaMemcpyDeviceToHost, s);
     CK(cudaStreamEndCapture(s, &g));

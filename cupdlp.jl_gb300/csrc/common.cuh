@@ -90,8 +90,8 @@ struct StepState {
   int target_in_chunk;
   int attempts_in_chunk;
   int max_attempts_in_chunk;
-  int constant_step;       // ConstantStepsizeParams: every attempt is accepted
   unsigned int arrive;     // CTAs of the dual kernel finished in this attempt
+  int constant_step;       // ConstantStepsizeParams: every attempt is accepted
   long long primal_spmv;   // attempts whose primal kernel also ran A'y (a commit)
   const double* pow_table; // [1-(k+1)^-r, 1+(k+1)^-g] for k < pow_table_len (device)
   long long pow_table_len;

@@ -177,12 +177,8 @@ struct Workspace {
                        dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(), sy.get(), skx.get(), st_dev.get(),
                        part_p.get(), part_p_split.get(), part_d.get(), part_d_split.get(), mode, direct};
   }
-  void launch_primal(int mode, cudaStream_t s) {
-    primal_step_kernel<T><<<plan_p.num_ctas, kBlock, 0, s>>>(primal_args(mode));
-  }
-  void launch_dual(int mode, cudaStream_t s) {
-    dual_step_kernel<T><<<plan_d.num_ctas, kBlock, 0, s>>>(dual_args(mode));
-  }
+  void launch_primal(int mode, cudaStream_t s) { launch_step(primal_step_kernel<T>, plan_p.num_ctas, s, primal_args(mode)); }
+  void launch_dual(int mode, cudaStream_t s) { launch_step(dual_step_kernel<T>, plan_d.num_ctas, s, dual_args(mode)); }
 
   void launch_pair(int mode, cudaStream_t s) {
     launch_primal(mode, s);

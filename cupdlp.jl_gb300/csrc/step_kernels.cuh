@@ -16,9 +16,10 @@
 //   dual_step_kernel:   [if the previous attempt was accepted] the y / Kx weighted sums;
 //       then K dx (tiles of A), the projected dual candidate, Kx + K dx into the other half
 //       of the double-buffered y / Kx, per-CTA interaction and ||dy||^2 partials; the last
-//       CTA of an instance to finish reduces that instance's partials in CTA order and
-//       takes the accept/reject and step-size decision, flipping the buffer parity on
-//       accept.
+//       CTA of an instance to finish reduces that instance's partials in a fixed order and
+//       takes the accept/reject and step-size decision, flipping the buffer parity on accept.
+//       (A separate decision kernel measured slower: one more kernel boundary per attempt
+//       costs more than this CTA's serial tail.)
 // Every CTA belongs to one instance; each warp owns whole tiles (row sums in registers,
 // the fused epilogue on its rows), so no barrier sits between a warp's loads and its
 // arithmetic, and latency is hidden by the many warps resident per SM. A split row's
@@ -40,6 +41,14 @@
 namespace gpdhg {
 
 enum StepMode : int { kStepNormal = 0, kStepCommitOnly = 1 };
+
+// Programmatic dependent launch (sm_90+): the step kernels are launched with the
+// programmatic-serialization attribute, so a kernel's CTAs may start while the previous
+// kernel finishes. Everything before pdl_wait() must read only constant data (the tile
+// plan); pdl_wait() returns once the previous kernel has completed and its writes are
+// visible (immediately when it was launched without the attribute).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
 
 template <class T>
 struct PrimalArgs {
@@ -76,7 +85,7 @@ struct DualArgs {
   T* kx1;
   T* sy;
   T* skx;
-  StepState* st;
+  StepState* st_mut;     // one per instance; the instance's last CTA updates it
   const double* part_p;
   const double* part_p_split;
   double* part_d;        // [interaction | ||dy||^2] per CTA (num_ctas each)
@@ -85,7 +94,7 @@ struct DualArgs {
   int direct;            // dx holds x^ and the row sums are K x^ (see above)
 };
 
-// One lane's epilogue inputs for its row of a tile (loaded one tile ahead).
+// One lane's epilogue inputs for its row of a tile (issued with the tile's matrix loads).
 template <class T>
 struct PrimalIn {
   T dx;  // dx (x^ in direct mode); K'y when no commit is pending
@@ -104,6 +113,11 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_ke
   __shared__ T wpart[kBlock / 32];
   __shared__ Tile tl[kTilesPerCtaMax];
   const int b = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // programmatic dependent launch: let the next kernel's CTAs launch once all of ours have
+  // started, stage the constant tile descriptors, and only then wait for the previous kernel
+  pdl_launch_dependents();
+  const int nt = stage_tiles(a.plan.tiles, a.plan.cta_tile_begin[b], a.plan.cta_tile_begin[b + 1], tl);
+  pdl_wait();
   const StepState* st = a.st + a.plan.cta_inst[b];
   if (st->done) return;
   const int pending = st->pending_commit;
@@ -113,7 +127,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_ke
   // step_size / primal_weight: one FP64 division per CTA (GB300's FP64 pipe is narrow)
   __shared__ double s_tto;
   if (threadIdx.x == 0) s_tto = st->tau / st->omega;
-  const int nt = stage_tiles(a.plan.tiles, a.plan.cta_tile_begin[b], a.plan.cta_tile_begin[b + 1], tl);
+  __syncthreads();
   const T w = (T)st->commit_weight;
   const T tto = (T)s_tto;
   const T* yg = st->parity ? a.y1 : a.y0;
@@ -187,12 +201,16 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_ke
   };
   TileLoad<T> L0;
   PrimalIn<T> E0;
-  if (nt == 1 && tl[0].e_log2 == kCtaLong) {
-    // one long row for the whole CTA; warp 0 finishes it
-    const Tile t = tl[0];
-    if (warp == 0) load_in(t, E0);
-    if (pending) cta_row_sum(a.At.col, a.At.val, yg, t, wpart, &rs_all[0][0]);
-    if (warp == 0) finish(t, E0);
+  if (nt > 0 && tl[0].e_log2 <= group_code(1)) {
+    // group tiles: 8 / W long rows, W warps each; the group's first warp finishes its row
+    const int W = 1 << group_log2(tl[0].e_log2);
+    const int q = warp / W, sub = warp % W;
+    const bool has = q < nt;
+    Tile t{};
+    if (has) t = tl[q];
+    if (has && sub == 0) load_in(t, E0);
+    if (pending) group_row_sum(a.At.col, a.At.val, yg, t, has, W, sub, wpart, rs);
+    if (has && sub == 0) finish(t, E0);
   } else {
     // each warp walks its tiles q = warp, warp + 8, ...: a tile's epilogue inputs, row
     // offsets, columns and values are all issued before any of them is used
@@ -217,19 +235,22 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_ke
   }
 }
 
-// Decision of take_step! for one attempt (thread 0 of the last CTA).
-__device__ __forceinline__ void step_decision(StepState* st, double inter_signed, double dx2, double dy2) {
-  st->total_iters += st->constant_step ? 0 : 1;
-  st->kkt_passes += 1.0;
-  st->attempts_in_chunk += 1;
-  const double omega = st->omega;
-  const double tau = st->tau;
+// Decision of take_step! for one attempt, on a copy of the instance's state (the caller
+// writes it back). f1 / f2 are the step-size factors (1 - (k+1)^-r), (1 + (k+1)^-g)
+// for the attempt counter after this attempt, fetched early by the caller (host table).
+__device__ __forceinline__ void step_decision(StepState& s, double f1, double f2, double inter_signed, double dx2,
+                                              double dy2) {
+  s.total_iters += s.constant_step ? 0 : 1;
+  s.kkt_passes += 1.0;
+  s.attempts_in_chunk += 1;
+  const double omega = s.omega;
+  const double tau = s.tau;
   const double inter = fabs(inter_signed);
   const double ndx = sqrt(dx2), ndy = sqrt(dy2);
   const double movement = 0.5 * omega * ndx * ndx + (0.5 / omega) * ndy * ndy;
   double limit;
   bool accept;
-  if (st->constant_step) {
+  if (s.constant_step) {
     limit = __longlong_as_double(0x7ff0000000000000LL);
     accept = true;
   } else {
@@ -237,9 +258,9 @@ __device__ __forceinline__ void step_decision(StepState* st, double inter_signed
       limit = movement / inter;
       if (movement == 0.0) {
         // :384-390: terminate at the next evaluation; tau is left as it is
-        st->numerical_error = 1;
-        st->done = 1;
-        st->pending_commit = 0;
+        s.numerical_error = 1;
+        s.done = 1;
+        s.pending_commit = 0;
         return;
       }
     } else {
@@ -247,43 +268,66 @@ __device__ __forceinline__ void step_decision(StepState* st, double inter_signed
     }
     accept = tau <= limit;
   }
-  st->last_limit = limit;
+  s.last_limit = limit;
   if (accept) {
-    st->parity ^= 1;
-    st->pending_commit = 1;
-    st->commit_weight = st->iter_start_tau;
-    st->count_primal += 1;
-    st->count_dual += 1;
-    st->sum_w_primal += st->iter_start_tau;
-    st->sum_w_dual += st->iter_start_tau;
-    st->accepted += 1;
-    st->accepted_in_chunk += 1;
+    s.parity ^= 1;
+    s.pending_commit = 1;
+    s.commit_weight = s.iter_start_tau;
+    s.count_primal += 1;
+    s.count_dual += 1;
+    s.sum_w_primal += s.iter_start_tau;
+    s.sum_w_dual += s.iter_start_tau;
+    s.accepted += 1;
+    s.accepted_in_chunk += 1;
   } else {
-    st->pending_commit = 0;
-    st->rejected += 1;
+    s.pending_commit = 0;
+    s.rejected += 1;
   }
-  if (!st->constant_step) {
-    // (1 - (k+1)^-r) and (1 + (k+1)^-g): from the host-computed table while it lasts
-    const long long k = st->total_iters;
-    double f1, f2;
-    if (st->pow_table && k < st->pow_table_len) {
-      f1 = st->pow_table[2 * k];
-      f2 = st->pow_table[2 * k + 1];
-    } else {
-      const double k1 = (double)(k + 1);
-      f1 = 1.0 - 1.0 / pow(k1, st->reduction_exponent);
-      f2 = 1.0 + 1.0 / pow(k1, st->growth_exponent);
-    }
+  if (!s.constant_step) {
     const double first = f1 * limit;
     const double second = f2 * tau;
-    st->tau = jmin(first, second);
+    s.tau = jmin(first, second);
   }
-  if (accept) st->iter_start_tau = st->tau;
-  if (st->accepted_in_chunk >= st->target_in_chunk || st->attempts_in_chunk >= st->max_attempts_in_chunk)
-    st->done = 1;
+  if (accept) s.iter_start_tau = s.tau;
+  if (s.accepted_in_chunk >= s.target_in_chunk || s.attempts_in_chunk >= s.max_attempts_in_chunk) s.done = 1;
 }
 
-// One lane's epilogue inputs for its row of a tile of A (loaded one tile ahead).
+// Step-size factors for attempt counter k (take_step!, :405-407): the host table while it
+// lasts, else the same formula on the device.
+__device__ __forceinline__ void step_factors(const StepState& s, long long k, double& f1, double& f2) {
+  if (s.pow_table && k < s.pow_table_len) {
+    f1 = __ldcg(s.pow_table + 2 * k);
+    f2 = __ldcg(s.pow_table + 2 * k + 1);
+  } else {
+    const double k1 = (double)(k + 1);
+    f1 = 1.0 - 1.0 / pow(k1, s.reduction_exponent);
+    f2 = 1.0 + 1.0 / pow(k1, s.growth_exponent);
+  }
+}
+
+// Sum of three values over the CTA in a fixed order (valid in thread 0); `sh` holds 3 x 32.
+__device__ __forceinline__ void block_sum3(double& a, double& b, double& c, double* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  a = warp_sum(a);
+  b = warp_sum(b);
+  c = warp_sum(c);
+  if (lane == 0) {
+    sh[wid] = a;
+    sh[32 + wid] = b;
+    sh[64 + wid] = c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    a = b = c = 0.0;
+    for (int w = 0; w < kBlock / 32; ++w) {
+      a += sh[w];
+      b += sh[32 + w];
+      c += sh[64 + w];
+    }
+  }
+}
+
+// One lane's epilogue inputs for its row of a tile of A (issued with the tile's matrix loads).
 template <class T>
 struct DualIn {
   T y;
@@ -297,13 +341,15 @@ template <class T>
 __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) dual_step_kernel(DualArgs<T> a) {
   __shared__ T rs_all[kBlock / 32][32];
   __shared__ double wsum[2][kBlock / 32];
-  __shared__ double red[32];
-  __shared__ int is_last;
   __shared__ T wpart[kBlock / 32];
   __shared__ Tile tl[kTilesPerCtaMax];
+  __shared__ double red3[3 * 32];
+  __shared__ int is_last;
   const int b = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int inst = a.plan.cta_inst[b];
-  StepState* st = a.st + inst;
+  pdl_launch_dependents();  // as in the primal kernel
+  const int nt = stage_tiles(a.plan.tiles, a.plan.cta_tile_begin[b], a.plan.cta_tile_begin[b + 1], tl);
+  pdl_wait();
+  const StepState* st = a.st_mut + a.plan.cta_inst[b];
   if (st->done) return;
   const int pending = st->pending_commit;
   const bool commit_only = a.mode == kStepCommitOnly;
@@ -311,7 +357,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) dual_step_kern
   const bool direct = a.direct != 0;
   __shared__ double s_od;
   if (threadIdx.x == 0) s_od = st->omega * st->tau;  // primal_weight * step_size
-  const int nt = stage_tiles(a.plan.tiles, a.plan.cta_tile_begin[b], a.plan.cta_tile_begin[b + 1], tl);
+  __syncthreads();
   const T w = (T)st->commit_weight;
   const T od = (T)s_od;
   const int p = st->parity;
@@ -372,11 +418,15 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) dual_step_kern
   };
   TileLoad<T> L0;
   DualIn<T> E0;
-  if (nt == 1 && tl[0].e_log2 == kCtaLong) {
-    const Tile t = tl[0];
-    if (warp == 0) load_in(t, E0);
-    if (!commit_only) cta_row_sum(a.A.col, a.A.val, a.dx, t, wpart, &rs_all[0][0]);
-    if (warp == 0) finish(t, E0);
+  if (nt > 0 && tl[0].e_log2 <= group_code(1)) {
+    const int W = 1 << group_log2(tl[0].e_log2);
+    const int q = warp / W, sub = warp % W;
+    const bool has = q < nt;
+    Tile t{};
+    if (has) t = tl[q];
+    if (has && sub == 0) load_in(t, E0);
+    if (!commit_only) group_row_sum(a.A.col, a.A.val, a.dx, t, has, W, sub, wpart, rs);
+    if (has && sub == 0) finish(t, E0);
   } else {
     for (int q = warp; q < nt; q += kBlock / 32) {
       const Tile t = tl[q];
@@ -396,55 +446,86 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) dual_step_kern
     }
   }
   __syncthreads();
+  const int inst = a.plan.cta_inst[b];
   const int c0 = a.plan.inst_cta_begin[inst], c1 = a.plan.inst_cta_begin[inst + 1];
   if (threadIdx.x == 0) {
     if (!commit_only) {
       double si = 0.0, sd = 0.0;
-      for (int q = 0; q < kBlock / 32; ++q) {
-        si += wsum[0][q];
-        sd += wsum[1][q];
+      for (int k = 0; k < kBlock / 32; ++k) {
+        si += wsum[0][k];
+        sd += wsum[1][k];
       }
       a.part_d[b] = si;
       a.part_d[a.plan.num_ctas + b] = sd;
     }
     __threadfence();
-    const unsigned prev = atomicAdd(&st->arrive, 1u);
+    const unsigned prev = atomicAdd(&a.st_mut[inst].arrive, 1u);
     is_last = (prev == (unsigned)(c1 - c0 - 1)) ? 1 : 0;
   }
   __syncthreads();
   if (!is_last) return;
-  __threadfence();
+  StepState* stw = a.st_mut + inst;
   if (commit_only) {
     if (threadIdx.x == 0) {
-      st->pending_commit = 0;
-      st->arrive = 0;
+      stw->pending_commit = 0;
+      stw->arrive = 0;
     }
     return;
   }
-  // the instance's partials in a fixed order: CTAs, then split rows
-  double si = 0.0, sd = 0.0, sx = 0.0;
-  for (int k = c0 + threadIdx.x; k < c1; k += kBlock) {
-    si += __ldcg(a.part_d + k);
-    sd += __ldcg(a.part_d + a.plan.num_ctas + k);
-  }
-  const int s0 = a.plan.inst_split_begin[inst], s1 = a.plan.inst_split_begin[inst + 1];
-  for (int k = s0 + threadIdx.x; k < s1; k += kBlock) {
-    si += __ldcg(a.part_d_split + 2 * k);
-    sd += __ldcg(a.part_d_split + 2 * k + 1);
-  }
-  const int p0 = a.p_cta_begin[inst], p1 = a.p_cta_begin[inst + 1];
-  for (int k = p0 + threadIdx.x; k < p1; k += kBlock) sx += __ldcg(a.part_p + k);
-  const int q0 = a.p_split_begin[inst], q1 = a.p_split_begin[inst + 1];
-  for (int k = q0 + threadIdx.x; k < q1; k += kBlock) sx += __ldcg(a.part_p_split + k);
-  si = block_sum(si, red);
-  sd = block_sum(sd, red);
-  sx = block_sum(sx, red);
+  // the instance's last CTA: thread 0 fetches the state and the step-size factors first, so
+  // those loads overlap the partial reductions; partials in a fixed order (dual CTAs, dual
+  // split rows, primal CTAs, primal split rows), each range's loads issued before its adds
+  __shared__ StepState s;
+  double f1 = 0.0, f2 = 0.0;
   if (threadIdx.x == 0) {
-    st->arrive = 0;
-    if (pending) st->primal_spmv += 1;
-    st->pending_commit = 0;
-    step_decision(st, si, sx, sd);
+    s = *stw;
+    step_factors(s, s.total_iters + (s.constant_step ? 0 : 1), f1, f2);
   }
+  constexpr int U = 8;
+  auto sum_range = [&](const double* p, int stride, int off, int rb, int re) {
+    double acc = 0.0;
+    for (int k0 = rb; k0 < re; k0 += U * kBlock) {
+      double v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int k = k0 + u * kBlock + (int)threadIdx.x;
+        v[u] = k < re ? __ldcg(p + (size_t)stride * k + off) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) acc += v[u];
+    }
+    return acc;
+  };
+  const int s0 = a.plan.inst_split_begin[inst], s1 = a.plan.inst_split_begin[inst + 1];
+  const int p0 = a.p_cta_begin[inst], p1 = a.p_cta_begin[inst + 1];
+  const int q0 = a.p_split_begin[inst], q1 = a.p_split_begin[inst + 1];
+  double si = sum_range(a.part_d, 1, 0, c0, c1) + sum_range(a.part_d_split, 2, 0, s0, s1);
+  double sd = sum_range(a.part_d + a.plan.num_ctas, 1, 0, c0, c1) + sum_range(a.part_d_split, 2, 1, s0, s1);
+  double sx = sum_range(a.part_p, 1, 0, p0, p1) + sum_range(a.part_p_split, 1, 0, q0, q1);
+  block_sum3(si, sd, sx, red3);
+  if (threadIdx.x == 0) {
+    s.arrive = 0;
+    if (pending) s.primal_spmv += 1;
+    s.pending_commit = 0;
+    step_decision(s, f1, f2, si, sx, sd);
+    *stw = s;
+  }
+}
+
+// Launches a step kernel with programmatic dependent launch enabled (see pdl_wait).
+template <class Args>
+inline void launch_step(void (*kernel)(Args), int grid, cudaStream_t s, const Args& args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(kBlock);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  CK(cudaLaunchKernelEx(&cfg, kernel, args));
 }
 
 }  // namespace gpdhg

@@ -11,23 +11,24 @@ namespace gpdhg {
 template <class T>
 struct TileLoad {
   int rpl;
-  int c[kTileEMax];
-  T v[kTileEMax];
+  int c[TileTraits<T>::kEMax];
+  T v[TileTraits<T>::kEMax];
 };
 
 // Issues the loads of tile t (none is used here, so all are in flight together).
 template <class T>
 __device__ __forceinline__ void tile_load(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
                                           const T* __restrict__ val, const Tile& t, TileLoad<T>& L) {
-  if (t.e_log2 < 0) return;  // a long row: streamed by long_row_sum / cta_row_sum
+  if (t.e_log2 < 0) return;  // a long row: streamed by long_row_sum / group_row_sum
   const int lane = threadIdx.x & 31;
   const int E = 1 << t.e_log2;
   const int kb = lane << t.e_log2;
   const int ke = min(t.nnz, kb + E);
   L.rpl = lane <= t.rows ? row_ptr[t.row_begin + lane] : 0;
 #pragma unroll
-  for (int j = 0; j < kTileEMax; ++j) {
-    const bool in = j < E && kb + j < ke;
+  for (int j = 0; j < TileTraits<T>::kEMax; ++j) {
+    if (j >= E) break;  // E is the same for the whole warp: a uniform exit, nothing issued past it
+    const bool in = kb + j < ke;
     L.c[j] = in ? lds(col + t.nnz_begin + kb + j) : 0;
     L.v[j] = in ? lds(val + t.nnz_begin + kb + j) : T(0);
   }
@@ -40,64 +41,61 @@ __device__ __forceinline__ void tile_load(const int32_t* __restrict__ row_ptr, c
 // crosses lanes is completed by a segmented shuffle scan of the lanes' trailing partial
 // sums. Every sum's order depends only on the tile, never on its position in memory. rs
 // (32 entries per warp) is complete after the final __syncwarp.
-// One row of up to kLongNnz nonzeros summed by the whole warp: rounds of 32 x kLongRound
-// coalesced (column, value) loads, all issued before the round's gathers, FMAs into four
-// independent accumulators per lane, then a fixed-order tree.
+// A warp's rounds r0, r0 + step, ... (< nnz) of a long row: 32 x kLongRound coalesced
+// (column, value) loads per round, all issued before the round's gathers, FMAs into four
+// independent accumulators. Returns the lane's sum (fixed order: accumulators added
+// pairwise). (Keeping two rounds in flight needed more registers than the kernels' occupancy
+// leaves and measured slower.)
+template <class T>
+__device__ __forceinline__ T stream_rounds(const int32_t* __restrict__ cp, const T* __restrict__ vp,
+                                           const T* __restrict__ xg, int nnz, int r0, int step) {
+  const int lane = threadIdx.x & 31;
+  T acc[4] = {T(0), T(0), T(0), T(0)};
+  for (; r0 < nnz; r0 += step) {
+    int c[kLongRound];
+    T v[kLongRound];
+#pragma unroll
+    for (int j = 0; j < kLongRound; ++j) {
+      const int k = r0 + j * 32 + lane;
+      c[j] = k < nnz ? lds(cp + k) : 0;
+      v[j] = k < nnz ? lds(vp + k) : T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < kLongRound; ++j)
+      if (r0 + j * 32 + lane < nnz) acc[j & 3] = fma(v[j], xg[c[j]], acc[j & 3]);
+  }
+  return (acc[0] + acc[1]) + (acc[2] + acc[3]);
+}
+
+// One row of up to kWarpShare nonzeros summed by the whole warp (valid in lane 0).
 template <class T>
 __device__ __forceinline__ T long_row_sum(const int32_t* __restrict__ col, const T* __restrict__ val,
                                           const T* __restrict__ xg, const Tile& t) {
-  const int lane = threadIdx.x & 31;
-  T acc[4] = {T(0), T(0), T(0), T(0)};
-  const int32_t* cp = col + t.nnz_begin;
-  const T* vp = val + t.nnz_begin;
-  for (int r0 = 0; r0 < t.nnz; r0 += 32 * kLongRound) {
-    int c[kLongRound];
-    T v[kLongRound];
-#pragma unroll
-    for (int j = 0; j < kLongRound; ++j) {
-      const int k = r0 + j * 32 + lane;
-      c[j] = k < t.nnz ? lds(cp + k) : 0;
-      v[j] = k < t.nnz ? lds(vp + k) : T(0);
-    }
-#pragma unroll
-    for (int j = 0; j < kLongRound; ++j)
-      if (r0 + j * 32 + lane < t.nnz) acc[j & 3] = fma(v[j], xg[c[j]], acc[j & 3]);
-  }
-  return warp_sum((acc[0] + acc[1]) + (acc[2] + acc[3]));  // valid in lane 0
+  return warp_sum(stream_rounds(col + t.nnz_begin, val + t.nnz_begin, xg, t.nnz, 0, 32 * kLongRound));
 }
 
-// One row (or piece) of a CTA tile summed by all 8 warps: warp w takes rounds w, w + 8, ...
-// of 32 x kLongRound coalesced nonzeros, then the warps' sums are added in warp order.
-// Every thread must call it; the sum is written to *out, valid after the final barrier.
+// Group tiles: the CTA's warps form groups of W = 2^g; group q sums tile q's row (or piece),
+// warp `sub` of the group streaming rounds sub, sub + W, ..., and the group's sums are added
+// in warp order. Every thread must call it (warps without a tile pass has = false); the row's
+// sum is in rs[0] of the group's first warp after the final __syncwarp.
 template <class T>
-__device__ __forceinline__ void cta_row_sum(const int32_t* __restrict__ col, const T* __restrict__ val,
-                                            const T* __restrict__ xg, const Tile& t, T* wpart, T* out) {
+__device__ __forceinline__ void group_row_sum(const int32_t* __restrict__ col, const T* __restrict__ val,
+                                              const T* __restrict__ xg, const Tile& t, bool has, int W, int sub,
+                                              T* wpart, T* rs) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  T acc[4] = {T(0), T(0), T(0), T(0)};
-  const int32_t* cp = col + t.nnz_begin;
-  const T* vp = val + t.nnz_begin;
-  for (int r0 = warp * 32 * kLongRound; r0 < t.nnz; r0 += kBlock * kLongRound) {
-    int c[kLongRound];
-    T v[kLongRound];
-#pragma unroll
-    for (int j = 0; j < kLongRound; ++j) {
-      const int k = r0 + j * 32 + lane;
-      c[j] = k < t.nnz ? lds(cp + k) : 0;
-      v[j] = k < t.nnz ? lds(vp + k) : T(0);
-    }
-#pragma unroll
-    for (int j = 0; j < kLongRound; ++j)
-      if (r0 + j * 32 + lane < t.nnz) acc[j & 3] = fma(v[j], xg[c[j]], acc[j & 3]);
-  }
-  const T ws = warp_sum((acc[0] + acc[1]) + (acc[2] + acc[3]));
+  T part = T(0);
+  if (has)
+    part = stream_rounds(col + t.nnz_begin, val + t.nnz_begin, xg, t.nnz, sub * 32 * kLongRound,
+                         W * 32 * kLongRound);
+  const T ws = warp_sum(part);
   if (lane == 0) wpart[warp] = ws;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (has && sub == 0 && lane == 0) {
     T s = T(0);
-    for (int w = 0; w < kBlock / 32; ++w) s += wpart[w];
-    *out = s;
+    for (int w = 0; w < W; ++w) s += wpart[warp + w];
+    rs[0] = s;
   }
-  __syncthreads();
+  __syncwarp();
 }
 
 template <class T>
@@ -119,9 +117,12 @@ __device__ __forceinline__ void tile_sums(const int32_t* __restrict__ col, const
     const int v = L.rpl - t.nnz_begin;
     rpl = v < 0 ? 0 : (v > t.nnz ? t.nnz : v);
   }
-  T xv[kTileEMax];
+  T xv[TileTraits<T>::kEMax];
 #pragma unroll
-  for (int j = 0; j < kTileEMax; ++j) xv[j] = (j < E && kb + j < ke) ? xg[L.c[j]] : T(0);
+  for (int j = 0; j < TileTraits<T>::kEMax; ++j) {
+    if (j >= E) break;
+    xv[j] = kb + j < ke ? xg[L.c[j]] : T(0);
+  }
   // first row whose end lies beyond kb (lane 0 starts at row 0: leading empty rows are its)
   int r;
   {
@@ -145,9 +146,10 @@ __device__ __forceinline__ void tile_sums(const int32_t* __restrict__ col, const
   T head_sum = T(0), tail_sum = T(0), s = T(0);
   bool tail_start = true;
 #pragma unroll
-  for (int j = 0; j < kTileEMax; ++j) {
+  for (int j = 0; j < TileTraits<T>::kEMax; ++j) {
+    if (j >= E) break;
     const int k = kb + j;
-    const bool in = active && j < E && k < ke;
+    const bool in = active && k < ke;
     while (true) {
       const bool need = in && k >= next;
       if (!__any_sync(full, need)) break;

@@ -13,8 +13,8 @@ int ceil_log2(long long v) {
 }
 }  // namespace
 
-void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t aux, std::vector<Tile>& out,
-                int32_t& splits, int32_t& carries) {
+void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t aux, int tile_nnz, int e_max,
+                std::vector<Tile>& out, int32_t& splits, int32_t& carries) {
   auto len = [&](int32_t r) { return (long long)rp[r + 1] - rp[r]; };
   auto push = [&](int32_t rb, int32_t rows, long long nb, long long nnz, int32_t split, int32_t piece,
                   int32_t pieces, int32_t carry) {
@@ -24,9 +24,9 @@ void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t
     t.nnz_begin = (int32_t)nb;
     t.nnz = (int32_t)nnz;
     // nonzeros per lane: enough for the tile, and about one row per lane when rows are
-    // short (fewer rows crossing lanes), at most kTileEMax
+    // short (fewer rows crossing lanes), at most e_max
     long long e = std::max<long long>(1, (nnz + 31) / 32);
-    if (rows > 0) e = std::max<long long>(e, std::min<long long>((nnz + rows - 1) / rows, kTileEMax));
+    if (rows > 0) e = std::max<long long>(e, std::min<long long>((nnz + rows - 1) / rows, e_max));
     t.e_log2 = ceil_log2(e);
     t.split = split;
     t.piece = piece;
@@ -39,13 +39,15 @@ void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t
   int32_t r = r0;
   while (r < r1) {
     const long long lr = len(r);
-    if (lr > kTileNnz) {
-      if (lr <= kLongNnz) {
+    if (lr > tile_nnz) {
+      if (lr <= kWarpShare) {
         push(r, 1, rp[r], lr, -1, 0, 1, 0);
         out.back().e_log2 = kWarpLong;
         ++r;
         continue;
       }
+      int g = 1;  // 2^g warps, about kWarpShare nonzeros each, at most 8
+      while (g < 3 && ((long long)kWarpShare << g) < lr) ++g;
       const int32_t pieces = (int32_t)((lr + kCtaNnz - 1) / kCtaNnz);
       int32_t sid = -1, cb = 0;
       if (pieces > 1) {
@@ -56,14 +58,14 @@ void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t
       for (int32_t q = 0; q < pieces; ++q) {
         push(r, 1, (long long)rp[r] + (long long)q * kCtaNnz,
              std::min<long long>(kCtaNnz, lr - (long long)q * kCtaNnz), sid, q, pieces, cb);
-        out.back().e_log2 = kCtaLong;
+        out.back().e_log2 = group_code(g);
       }
       ++r;
       continue;
     }
     const int32_t start = r;
     long long nnz = 0;
-    while (r < r1 && r - start < kTileRows && len(r) <= kTileNnz && nnz + len(r) <= kTileNnz) {
+    while (r < r1 && r - start < kTileRows && len(r) <= tile_nnz && nnz + len(r) <= tile_nnz) {
       nnz += len(r);
       ++r;
     }
@@ -84,21 +86,26 @@ void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector
     inst_cta[k] = (int32_t)cta_inst.size();
     inst_split[k] = splits;
     const size_t t0 = tiles.size();
-    list_tiles(M.host_rp.data(), bounds[k], bounds[k + 1], k, aux.empty() ? 0 : aux[k], tiles, splits, carries);
-    // CTAs: a CTA tile alone; other consecutive tiles of this instance in groups of tpc,
-    // where tpc grows from 8 to 32 once the instance has more than ~1,200 tiles (8 CTAs
-    // per SM of 152)
+    list_tiles(M.host_rp.data(), bounds[k], bounds[k + 1], k, aux.empty() ? 0 : aux[k], TileTraits<T>::kNnz,
+               TileTraits<T>::kEMax, tiles, splits, carries);
+    // CTAs: 8 / W group tiles of one width W together; other consecutive tiles of this
+    // instance in groups of tpc, where tpc grows from 8 to 32 once the instance has more than
+    // ~1,200 tiles (8 CTAs per SM of 152)
     const long long nt = (long long)(tiles.size() - t0);
     const long long tpc = std::min<long long>(kTilesPerCtaMax, std::max<long long>(kTilesPerCtaMin, (nt + 1215) / 1216));
-    long long open = 0;  // tiles in the CTA being filled
+    long long open = 0;   // tiles in the CTA being filled
+    int open_code = 0;    // its tiles' kind: 0 normal, else the group code
     for (size_t q = t0; q < tiles.size(); ++q) {
-      const bool cta_tile = tiles[q].e_log2 == kCtaLong;
-      if (cta_tile || open == 0 || open == tpc) {
+      const int e = tiles[q].e_log2;
+      const int code = e <= group_code(1) ? e : 0;
+      const long long cap = code ? (8 >> group_log2(code)) : tpc;
+      if (open == 0 || code != open_code || open == cap) {
         cta_begin.push_back((int32_t)q);
         cta_inst.push_back(k);
         open = 0;
+        open_code = code;
       }
-      open = cta_tile ? tpc : open + 1;  // nothing joins a CTA tile
+      ++open;
     }
   }
   inst_cta[K] = (int32_t)cta_inst.size();

@@ -1,15 +1,17 @@
 // tiles.h — the work decomposition of the step kernels: warp tiles grouped into CTAs.
 //
-// A tile is one warp's share of a CSR matrix: consecutive rows holding at most kTileNnz
-// nonzeros and at most kTileRows rows, or one row of up to kLongNnz nonzeros streamed by
-// the warp in rounds. A longer row is a CTA tile: a CTA of its own whose 8 warps split
-// the row and combine their sums in shared memory; a row longer than kCtaNnz is cut into
-// CTA pieces of kCtaNnz whose partial sums meet in a carry array. Consecutive tiles of
-// one instance form a CTA's work (8 to 32 tiles, dealt to its 8 warps in turn), so
-// every CTA belongs to exactly one instance and the per-instance step decision can count
-// CTAs. An instance with few tiles gets one tile per warp (most CTAs in flight), a large one
-// up to four per warp (fewer partial sums for the step decision to reduce). The decomposition depends only on the instance's own row lengths, never on where
-// the instance sits in a packed batch.
+// A tile is one warp's share of a CSR matrix: consecutive rows holding at most
+// TileTraits<T>::kNnz nonzeros and at most kTileRows rows, or one row of up to kWarpShare
+// nonzeros streamed by the warp in rounds. A longer row is a group tile: W = 2, 4 or 8
+// warps (about kWarpShare nonzeros each) split it and combine their sums in shared memory,
+// 8 / W such rows to a CTA; a row longer than kCtaNnz is cut into 8-warp pieces of kCtaNnz
+// whose partial sums meet in a carry array. Consecutive tiles of one instance form a CTA's
+// work (8 to 32 tiles, dealt to its 8 warps in turn, or 8 / W group tiles), so every CTA
+// belongs to exactly one instance and the per-instance step decision can count CTAs. An
+// instance with few tiles gets one tile per warp (most CTAs in flight), a large one up to
+// four per warp (fewer partial sums for the step decision to reduce). The decomposition
+// depends only on the instance's own row lengths, never on where the instance sits in a
+// packed batch.
 #pragma once
 
 #include <vector>
@@ -18,17 +20,24 @@
 
 namespace gpdhg {
 
-constexpr int kTileNnz = 256;     // nonzeros per tile (32 lanes x at most 8)
 constexpr int kTileRows = 31;     // rows per tile: rows + 1 row offsets fit in 32 lanes
-constexpr int kTileEMax = 8;      // nonzeros per lane
-constexpr int kLongNnz = 1024;    // longest row one warp streams alone
+// Nonzeros per lane (at most) and per tile: FP64 tiles are half as long, which keeps a
+// lane's values and gathered entries in registers at the FP64 kernels' occupancy.
+template <class T>
+struct TileTraits {
+  static constexpr int kEMax = sizeof(T) == 8 ? 4 : 8;
+  static constexpr int kNnz = 32 * kEMax;
+};
+constexpr int kWarpShare = 512;   // nonzeros per warp of a long row
 constexpr int kCtaNnz = 16384;    // longest row (piece) one CTA sums
 constexpr int kLongRound = 8;     // (column, value) loads per lane and round of a long row
 constexpr int kTilesPerCtaMin = 8;   // tiles per CTA: one per warp for small instances,
 constexpr int kTilesPerCtaMax = 32;  // up to four per warp for large ones
 
-constexpr int kWarpLong = -1;
-constexpr int kCtaLong = -2;
+constexpr int kWarpLong = -1;  // Tile::e_log2 of a row streamed by one warp
+// Tile::e_log2 of a row summed by 2^g warps (g = 1, 2, 3)
+__host__ __device__ constexpr int group_code(int g) { return -1 - g; }
+__host__ __device__ constexpr int group_log2(int e_log2) { return -1 - e_log2; }
 
 struct Tile {
   int32_t row_begin;  // first row (packed numbering)
@@ -36,7 +45,7 @@ struct Tile {
   int32_t nnz_begin;  // first nonzero in the CSR
   int32_t nnz;        // nonzeros of the tile
   int32_t e_log2;     // log2 of the nonzeros per lane; kWarpLong: one row streamed by the
-                      // warp; kCtaLong: one row (or piece) summed by a whole CTA
+                      // warp; group_code(g): one row (or piece) summed by 2^g warps
   int32_t split;      // -1, or the split row this piece belongs to
   int32_t piece;      // piece index within the split row
   int32_t pieces;     // pieces of the split row
@@ -74,8 +83,8 @@ struct TilePlan {
 
 // Appends the tiles of rows [r0, r1) of a CSR with row pointer rp (instance inst). An empty
 // range still gets one empty tile (the instance's step decision runs in its CTA).
-void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t aux, std::vector<Tile>& out,
-                int32_t& splits, int32_t& carries);
+void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t aux, int tile_nnz, int e_max,
+                std::vector<Tile>& out, int32_t& splits, int32_t& carries);
 
 // Plan of rows [bounds[k], bounds[k + 1]) for every instance k of matrix M (Tile::aux =
 // aux[k], or 0 when aux is empty).
