@@ -142,6 +142,38 @@ gpdhg_status gpdhg_solve(gpdhg_problem* p, const gpdhg_params* params, gpdhg_res
   });
 }
 
+gpdhg_status gpdhg_problem_create_unscaled(const gpdhg_lp_desc* desc, const gpdhg_params* params,
+                                           gpdhg_problem** out) {
+  return guarded([&] {
+    if (!out) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (!desc || !params) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "desc or params is NULL");
+    if (desc->original_variable_lower_bound || desc->original_variable_upper_bound ||
+        desc->original_objective_vector || desc->original_right_hand_side || desc->constraint_rescaling ||
+        desc->variable_rescaling)
+      throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT,
+                         "an unscaled descriptor carries no original_* or rescaling vectors");
+    if (params->l_inf_ruiz_iterations < 0)
+      throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "l_inf_ruiz_iterations must be >= 0");
+    gpdhg_problem* p = new gpdhg_problem();
+    try {
+      gpdhg::problem_init(p, desc);
+      gpdhg::rescale_on_device(p, *params);
+    } catch (...) {
+      delete p;
+      throw;
+    }
+    *out = p;
+  });
+}
+
+gpdhg_status gpdhg_get_rescaling(const gpdhg_problem* p, double* constraint_rescaling, double* variable_rescaling) {
+  return guarded([&] {
+    if (!p) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "problem is NULL");
+    gpdhg::get_rescaling(p, constraint_rescaling, variable_rescaling);
+  });
+}
+
 gpdhg_status gpdhg_get_stats(const gpdhg_problem* p, int32_t index, gpdhg_iteration_stats* out) {
   return guarded([&] {
     if (!p || !out) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "problem or out is NULL");

@@ -134,4 +134,9 @@ void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d);
 void launch_convert_d2f(const double* src, float* dst, long long n, cudaStream_t s);
 // Ensures FP32 copies of the matrix values exist.
 void ensure_fp32_values(gpdhg_problem* p);
+// rescale_problem on the device (rescale.cu): rescales a problem built from an unscaled
+// descriptor in place and recomputes its scaled host scalars.
+void rescale_on_device(gpdhg_problem* p, const gpdhg_params& prm);
+// Copies the constraint (m) and variable (n) rescaling vectors to the host.
+void get_rescaling(const gpdhg_problem* p, double* con, double* var);
 }  // namespace gpdhg
