@@ -206,6 +206,9 @@ struct BatchWorkspace {
   PinnedBuf<double> red_host;
   TilePlan<T> plan_p, plan_d;   // tiles of the packed A' and A, instance by instance
   DBuf<double> part_p_split, part_d_split;
+  // launched CTAs: those of instances not yet retired (rebuilt when their count halves)
+  DBuf<int32_t> map_p, map_d;
+  int grid_p = 0, grid_d = 0;
   DBuf<uint8_t> flags;             // 4 x count: active, use_current, to_avg, restart
   PinnedBuf<uint8_t> flags_host;
   cudaGraphExec_t graphs[kBatchLevels] = {};
@@ -262,24 +265,73 @@ struct BatchWorkspace {
     red_part.alloc((size_t)16 * std::max(B->nseg_n, B->nseg_m));
     red_out.alloc((size_t)count * 32);
     flags.alloc(4 * (size_t)count);
-    for (int lv = 0; lv < kBatchLevels; ++lv) graphs[lv] = capture(1 << lv);
+    compact(std::vector<char>(count, 0));
   }
   ~BatchWorkspace() {
     for (cudaGraphExec_t g : graphs)
       if (g) cudaGraphExecDestroy(g);
   }
+  TileView<T> view_p() const {
+    TileView<T> v = plan_p.view();
+    v.cta_map = map_p.get();
+    return v;
+  }
+  TileView<T> view_d() const {
+    TileView<T> v = plan_d.view();
+    v.cta_map = map_d.get();
+    return v;
+  }
+  // Launches only the CTAs of instances that are not retired; re-captures the step graphs.
+  std::vector<int32_t> hbeg_p, hbeg_d;  // host copies of the plans' per-instance CTA ranges
+  // CTAs the step kernels would launch with the given retirements (primal plan)
+  int active_ctas(const std::vector<char>& retired) const {
+    int a = 0;
+    for (int k = 0; k < count; ++k)
+      if (!retired[k]) a += hbeg_p[k + 1] - hbeg_p[k];
+    return a;
+  }
+  void compact(const std::vector<char>& retired) {
+    if (hbeg_p.empty()) {
+      hbeg_p.resize(count + 1);
+      hbeg_d.resize(count + 1);
+      CK(cudaMemcpy(hbeg_p.data(), plan_p.inst_cta_begin.get(), sizeof(int32_t) * (count + 1), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(hbeg_d.data(), plan_d.inst_cta_begin.get(), sizeof(int32_t) * (count + 1), cudaMemcpyDeviceToHost));
+    }
+    std::vector<int32_t> mp, md;
+    auto collect = [&](const std::vector<int32_t>& begin, std::vector<int32_t>& map) {
+      for (int k = 0; k < count; ++k)
+        if (!retired[k])
+          for (int32_t c0 = begin[k]; c0 < begin[k + 1]; ++c0) map.push_back(c0);
+    };
+    collect(hbeg_p, mp);
+    collect(hbeg_d, md);
+    if (mp.empty() || md.empty()) return;  // nothing runs any more
+    auto up = [&](DBuf<int32_t>& d, const std::vector<int32_t>& v) {
+      d.alloc(v.size());
+      CK(cudaMemcpy(d.get(), v.data(), sizeof(int32_t) * v.size(), cudaMemcpyHostToDevice));
+    };
+    up(map_p, mp);
+    up(map_d, md);
+    grid_p = (int)mp.size();
+    grid_d = (int)md.size();
+    for (cudaGraphExec_t& g : graphs) {
+      if (g) cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+    for (int lv = 0; lv < kBatchLevels; ++lv) graphs[lv] = capture(1 << lv);
+  }
   PrimalArgs<T> pargs(int mode) {
-    return PrimalArgs<T>{B->At.view<T>(), plan_p.view(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(),
+    return PrimalArgs<T>{B->At.view<T>(), view_p(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(),
                          skty.get(), y0.get(), y1.get(), st_dev.get(), part_p.get(), part_p_split.get(), mode, direct};
   }
   DualArgs<T> dargs(int mode) {
-    return DualArgs<T>{B->A.view<T>(), plan_d.view(), plan_p.inst_cta_begin.get(), plan_p.inst_split_begin.get(),
+    return DualArgs<T>{B->A.view<T>(), view_d(), plan_p.inst_cta_begin.get(), plan_p.inst_split_begin.get(),
                        dx.get(), b, y0.get(), y1.get(), kx0.get(), kx1.get(), sy.get(), skx.get(), st_dev.get(),
                        part_p.get(), part_p_split.get(), part_d.get(), part_d_split.get(), mode, direct};
   }
   void launch_pair(int mode, cudaStream_t s) {
-    launch_step(primal_step_kernel<T>, plan_p.num_ctas, s, pargs(mode));
-    launch_step(dual_step_kernel<T>, plan_d.num_ctas, s, dargs(mode));
+    launch_step(primal_step_kernel<T>, grid_p, s, pargs(mode));
+    launch_step(dual_step_kernel<T>, grid_d, s, dargs(mode));
     launches += 2;
   }
   void launch_pair(int mode) { launch_pair(mode, B->stream); }
@@ -288,8 +340,8 @@ struct BatchWorkspace {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < pairs; ++k) {
-      launch_step(primal_step_kernel<T>, plan_p.num_ctas, s, pargs(kStepNormal));
-      launch_step(dual_step_kernel<T>, plan_d.num_ctas, s, dargs(kStepNormal));
+      launch_step(primal_step_kernel<T>, grid_p, s, pargs(kStepNormal));
+      launch_step(dual_step_kernel<T>, grid_d, s, dargs(kStepNormal));
     }
     cudaMemcpyAsync(st_host.p, st_dev.get(), sizeof(StepState) * count, cudaMemcpyDeviceToHost, s);
     CK(cudaStreamEndCapture(s, &g));
@@ -341,6 +393,7 @@ static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& 
   const long long freq = std::max(1, prm.termination_evaluation_frequency);
   const long long it_limit = prm.iteration_limit;
   const long long launches0 = W.launches;
+  if (W.grid_p != W.plan_p.num_ctas) W.compact(std::vector<char>(K, 0));  // a new solve: every instance runs
   // initial state (:494-611) for every instance
   for (DBuf<T>* v : {&W.x, &W.kty, &W.sx, &W.skty, &W.dx, &W.ax, &W.agrad, &W.rx})
     CK(cudaMemsetAsync(v->get(), 0, sizeof(T) * v->n, s));
@@ -552,6 +605,8 @@ static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& 
       }
     }
     if (alive == 0) break;
+    // launch only the CTAs of running instances once retirements have halved them
+    if (2 * W.active_ctas(retired) < W.grid_p) W.compact(retired);
     // ---- step graphs until every running instance reached its evaluation point ----
     W.push_state();
     const auto tb = Clock::now();

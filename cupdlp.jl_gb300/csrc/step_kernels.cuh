@@ -112,7 +112,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_ke
   __shared__ double wsum[kBlock / 32];
   __shared__ T wpart[kBlock / 32];
   __shared__ Tile tl[kTilesPerCtaMax];
-  const int b = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = a.plan.cta_map ? a.plan.cta_map[blockIdx.x] : (int)blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // programmatic dependent launch: let the next kernel's CTAs launch once all of ours have
   // started, stage the constant tile descriptors, and only then wait for the previous kernel
   pdl_launch_dependents();
@@ -345,7 +346,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) dual_step_kern
   __shared__ Tile tl[kTilesPerCtaMax];
   __shared__ double red3[3 * 32];
   __shared__ int is_last;
-  const int b = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = a.plan.cta_map ? a.plan.cta_map[blockIdx.x] : (int)blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   pdl_launch_dependents();  // as in the primal kernel
   const int nt = stage_tiles(a.plan.tiles, a.plan.cta_tile_begin[b], a.plan.cta_tile_begin[b + 1], tl);
   pdl_wait();

@@ -63,6 +63,8 @@ struct TileView {
   const int32_t* inst_split_begin;  // first split row of each instance (instances + 1)
   T* carry;                         // one partial row sum per piece of every split row
   unsigned* counter;                // pieces finished per split row (back to 0 after each launch)
+  const int32_t* cta_map;           // launched CTA -> plan CTA (NULL: the identity); a batch
+                                    // launches only the CTAs of instances still running
   int32_t num_ctas;
   int32_t num_splits;
 };
@@ -76,8 +78,8 @@ struct TilePlan {
   int32_t num_tiles = 0, num_ctas = 0, num_splits = 0;
   TileView<T> view() const {
     return TileView<T>{tiles.get(),      cta_tile_begin.get(), cta_inst.get(), inst_cta_begin.get(),
-                       inst_split_begin.get(), carry.get(),     counter.get(),  num_ctas,
-                       num_splits};
+                       inst_split_begin.get(), carry.get(),     counter.get(),  nullptr,
+                       num_ctas,               num_splits};
   }
 };
 
