@@ -339,7 +339,7 @@ struct DualIn {
 };
 
 template <class T>
-__global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) dual_step_kernel(DualArgs<T> a) {
+__global__ void __launch_bounds__(kBlock, 4) dual_step_kernel(DualArgs<T> a) {
   __shared__ T rs_all[kBlock / 32][32];
   __shared__ double wsum[2][kBlock / 32];
   __shared__ T wpart[kBlock / 32];
@@ -475,35 +475,43 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) dual_step_kern
     return;
   }
   // the instance's last CTA: thread 0 fetches the state and the step-size factors first, so
-  // those loads overlap the partial reductions; partials in a fixed order (dual CTAs, dual
-  // split rows, primal CTAs, primal split rows), each range's loads issued before its adds
+  // those loads overlap the partial reductions; partials in a fixed order
   __shared__ StepState s;
   double f1 = 0.0, f2 = 0.0;
   if (threadIdx.x == 0) {
     s = *stw;
     step_factors(s, s.total_iters + (s.constant_step ? 0 : 1), f1, f2);
   }
-  constexpr int U = 8;
-  auto sum_range = [&](const double* p, int stride, int off, int rb, int re) {
-    double acc = 0.0;
-    for (int k0 = rb; k0 < re; k0 += U * kBlock) {
-      double v[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int k = k0 + u * kBlock + (int)threadIdx.x;
-        v[u] = k < re ? __ldcg(p + (size_t)stride * k + off) : 0.0;
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) acc += v[u];
-    }
-    return acc;
-  };
+  // one round of loads for the three CTA ranges (dual interaction, dual ||dy||^2, primal
+  // ||dx||^2), all issued before any is added; split-row slots (rare) follow
+  constexpr int U = 4;
   const int s0 = a.plan.inst_split_begin[inst], s1 = a.plan.inst_split_begin[inst + 1];
   const int p0 = a.p_cta_begin[inst], p1 = a.p_cta_begin[inst + 1];
   const int q0 = a.p_split_begin[inst], q1 = a.p_split_begin[inst + 1];
-  double si = sum_range(a.part_d, 1, 0, c0, c1) + sum_range(a.part_d_split, 2, 0, s0, s1);
-  double sd = sum_range(a.part_d + a.plan.num_ctas, 1, 0, c0, c1) + sum_range(a.part_d_split, 2, 1, s0, s1);
-  double sx = sum_range(a.part_p, 1, 0, p0, p1) + sum_range(a.part_p_split, 1, 0, q0, q1);
+  const int span = max(c1 - c0, p1 - p0);
+  double si = 0.0, sd = 0.0, sx = 0.0;
+  for (int k0 = (int)threadIdx.x; k0 < span; k0 += U * kBlock) {
+    double vi[U], vd[U], vx[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int k = k0 + u * kBlock;
+      const bool ind = c0 + k < c1, inp = p0 + k < p1;
+      vi[u] = ind ? __ldcg(a.part_d + c0 + k) : 0.0;
+      vd[u] = ind ? __ldcg(a.part_d + a.plan.num_ctas + c0 + k) : 0.0;
+      vx[u] = inp ? __ldcg(a.part_p + p0 + k) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      si += vi[u];
+      sd += vd[u];
+      sx += vx[u];
+    }
+  }
+  for (int k = s0 + threadIdx.x; k < s1; k += kBlock) {
+    si += __ldcg(a.part_d_split + 2 * k);
+    sd += __ldcg(a.part_d_split + 2 * k + 1);
+  }
+  for (int k = q0 + threadIdx.x; k < q1; k += kBlock) sx += __ldcg(a.part_p_split + k);
   block_sum3(si, sd, sx, red3);
   if (threadIdx.x == 0) {
     s.arrive = 0;
