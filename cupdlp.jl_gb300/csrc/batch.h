@@ -10,7 +10,7 @@
 
 namespace gpdhg {
 
-constexpr int kSegLen = 4096;   // elements per segmented-reduction item
+constexpr int kSegLen = 1024;   // elements per segmented-reduction item (one CTA each)
 
 template <class T>
 struct BatchWorkspace;

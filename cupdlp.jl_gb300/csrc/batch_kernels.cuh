@@ -20,38 +20,37 @@ namespace gpdhg {
 template <int Q, unsigned MAXMASK, class F>
 __global__ void __launch_bounds__(kBlock) seg_reduce_kernel(const SegItem* items, const uint8_t* active, F f,
                                                             double* partials, int num_items) {
-  __shared__ double sh[32];
+  __shared__ double sh[Q][kBlock / 32];
   const SegItem it = items[blockIdx.x];
   if (!active[it.inst]) return;
   double acc[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) acc[q] = 0.0;
   for (int i = it.begin + threadIdx.x; i < it.end; i += kBlock) f((long long)i, acc);
-#pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    const double r = ((MAXMASK >> q) & 1u) ? block_nan_max(acc[q], sh) : block_sum(acc[q], sh);
-    if (threadIdx.x == 0) partials[(size_t)q * num_items + blockIdx.x] = r;
-  }
+  const double r = block_reduce_q<Q, MAXMASK>(acc, sh);
+  if ((int)threadIdx.x < Q) partials[(size_t)threadIdx.x * num_items + blockIdx.x] = r;
 }
 
 template <int Q, unsigned MAXMASK>
 __global__ void __launch_bounds__(kBlock) seg_finalize_kernel(const int32_t* inst_item_begin, const uint8_t* active,
                                                               const double* partials, int num_items, double* out,
                                                               int out_stride) {
-  __shared__ double sh[32];
+  __shared__ double sh[Q][kBlock / 32];
   const int inst = blockIdx.x;
   if (!active[inst]) return;
   const int k0 = inst_item_begin[inst], k1 = inst_item_begin[inst + 1];
-  for (int q = 0; q < Q; ++q) {
-    const bool is_max = (MAXMASK >> q) & 1u;
-    double a = 0.0;
-    for (int k = k0 + threadIdx.x; k < k1; k += kBlock) {
+  double acc[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) acc[q] = 0.0;
+  for (int k = k0 + threadIdx.x; k < k1; k += kBlock) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
       const double v = partials[(size_t)q * num_items + k];
-      a = is_max ? nan_max(a, v) : a + v;
+      acc[q] = ((MAXMASK >> q) & 1u) ? nan_max(acc[q], v) : acc[q] + v;
     }
-    a = is_max ? block_nan_max(a, sh) : block_sum(a, sh);
-    if (threadIdx.x == 0) out[(size_t)inst * out_stride + q] = a;
   }
+  const double r = block_reduce_q<Q, MAXMASK>(acc, sh);
+  if ((int)threadIdx.x < Q) out[(size_t)inst * out_stride + threadIdx.x] = r;
 }
 
 // Per-element helpers driven by per-instance flags / weights.

@@ -3,16 +3,40 @@
 // The reference computes each statistic with its own broadcast kernel and a host
 // round trip per norm, and allocates temporaries for concatenated norms
 // (src/iteration_stats_utils_gpu.jl:23-372, src/saddle_point_gpu.jl:250-278). Here every
-// statistic of one evaluation is accumulated in FP64 in a single grid-stride pass per
-// side (n columns, m rows), into per-CTA partials that one finalize CTA reduces in a
-// fixed order; the host reads back one small array.
+// statistic of one evaluation is accumulated in FP64 in a single pass per side (n columns,
+// m rows) over fixed segments (batch_kernels.cuh), into per-segment partials that one
+// finalize CTA per instance reduces in a fixed order; the host reads back one small array.
+// Comparisons, maxima and sign tests run on the integer pipe (bit patterns), so the FP64
+// pipe only does the arithmetic itself.
 #pragma once
 
 #include "common.cuh"
 
 namespace gpdhg {
 
-__device__ __forceinline__ double nan_max(double a, double b) { return (a != a || b != b) ? a + b : fmax(a, b); }
+// The evaluation's max-quantities are all magnitudes (|v|, or a positive part): their
+// NaN-propagating maximum is the integer maximum of the bit patterns with the sign cleared
+// (+0 < ... < +inf < NaN), done on the integer pipe instead of GB300's narrow FP64 pipe.
+__device__ __forceinline__ double nan_max(double a, double b) {
+  const unsigned long long ua = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffULL;
+  const unsigned long long ub = (unsigned long long)__double_as_longlong(b) & 0x7fffffffffffffffULL;
+  return __longlong_as_double((long long)(ua > ub ? ua : ub));
+}
+
+__device__ __forceinline__ bool bits_nan(long long b) { return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+
+// Julia's max(v, 0) and min(v, 0) (NaN-propagating), by sign and NaN tests on the bits.
+__device__ __forceinline__ double pos_part(double v) {
+  const long long b = __double_as_longlong(v);
+  return (b > 0 || bits_nan(b)) ? v : 0.0;  // +x (x != 0) and NaN kept; -x, -0, +0 -> +0
+}
+__device__ __forceinline__ double neg_part(double v) {
+  const long long b = __double_as_longlong(v);
+  return ((b < 0 && (b & 0x7fffffffffffffffLL) != 0) || bits_nan(b)) ? v : 0.0;
+}
+__device__ __forceinline__ bool bits_finite(double v) {
+  return (__double_as_longlong(v) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
+}
 
 __device__ __forceinline__ double warp_nan_max(double v) {
 #pragma unroll
@@ -34,45 +58,40 @@ __device__ __forceinline__ double block_nan_max(double v, double* sh) {
   return r;
 }
 
-// Grid-stride reduction of Q quantities; bit q of MAXMASK selects max (else sum).
-// All max-quantities are magnitudes, so 0 is their identity.
-template <int Q, unsigned MAXMASK, class F>
-__global__ void __launch_bounds__(kBlock) reduce_kernel(long long len, F f, double* partials) {
-  __shared__ double sh[32];
-  double acc[Q];
-#pragma unroll
-  for (int q = 0; q < Q; ++q) acc[q] = 0.0;
-  const long long stride = (long long)gridDim.x * kBlock;
-  for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < len; i += stride) f(i, acc);
-#pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    const double r = ((MAXMASK >> q) & 1u) ? block_nan_max(acc[q], sh) : block_sum(acc[q], sh);
-    if (threadIdx.x == 0) partials[q * gridDim.x + blockIdx.x] = r;
-  }
-}
-
+// Q per-thread accumulators reduced over the CTA with one barrier: each warp reduces all Q
+// (shuffle trees), then thread q < Q combines the warps' values for quantity q in warp order.
+// Bit q of MAXMASK selects max (else sum). The result for q is valid in thread q.
 template <int Q, unsigned MAXMASK>
-__global__ void __launch_bounds__(kBlock) finalize_kernel(const double* partials, int nb, double* out) {
-  __shared__ double sh[32];
+__device__ __forceinline__ double block_reduce_q(double* acc, double (*sh)[kBlock / 32]) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
   for (int q = 0; q < Q; ++q) {
-    const bool is_max = (MAXMASK >> q) & 1u;
-    double a = 0.0;
-    for (int k = threadIdx.x; k < nb; k += kBlock) {
-      const double v = partials[q * nb + k];
-      a = is_max ? nan_max(a, v) : a + v;
-    }
-    a = is_max ? block_nan_max(a, sh) : block_sum(a, sh);
-    if (threadIdx.x == 0) out[q] = a;
+    const double v = ((MAXMASK >> q) & 1u) ? warp_nan_max(acc[q]) : warp_sum(acc[q]);
+    if (lane == 0) sh[q][wid] = v;
   }
+  __syncthreads();
+  double r = 0.0;
+  if ((int)threadIdx.x < Q) {
+    const int q = threadIdx.x;
+    const bool is_max = (MAXMASK >> q) & 1u;
+    for (int w = 0; w < kBlock / 32; ++w) r = is_max ? nan_max(r, sh[q][w]) : r + sh[q][w];
+  }
+  return r;
 }
 
 __device__ __forceinline__ double reduced_cost(double g, bool fl, bool fu) {
-  // src/iteration_stats_utils_gpu.jl:168: max(g,0)*isfinite(l) + min(g,0)*isfinite(u)
-  return (fl ? jmax(g, 0.0) : 0.0) + (fu ? jmin(g, 0.0) : 0.0);
+  // src/iteration_stats_utils_gpu.jl:168: max(g,0)*isfinite(l) + min(g,0)*isfinite(u). At
+  // most one term is nonzero unless g is NaN (then the sum is NaN), so the sum is a select.
+  const double p = fl ? pos_part(g) : 0.0;
+  const double q = fu ? neg_part(g) : 0.0;
+  const long long bp = __double_as_longlong(p);
+  return (bp != 0) ? p : q;  // p is +0 or a positive value / NaN
 }
 __device__ __forceinline__ double rc_contribution(double rc, double l, double u) {
-  // src/iteration_stats_utils_gpu.jl:120-126
-  return rc > 0.0 ? l * rc : (rc < 0.0 ? u * rc : 0.0);
+  // src/iteration_stats_utils_gpu.jl:120-126 (rc > 0, rc < 0 tested on the bits)
+  const long long b = __double_as_longlong(rc);
+  if (bits_nan(b) || (b & 0x7fffffffffffffffLL) == 0) return 0.0;  // neither rc > 0 nor rc < 0
+  return b > 0 ? l * rc : u * rc;
 }
 
 // Unscaled primal-side statistics of the averaged iterate (original problem).
@@ -95,8 +114,8 @@ struct EvalN {
     const double x = (double)ax[j] / var[j];       // :470-471
     const double g = (double)agrad[j] * var[j];    // :472-473
     const double l = ol[j], u = ou[j], c = oc[j];
-    const bool fl = isfinite(l), fu = isfinite(u);
-    const double lv = jmax(l - x, 0.0), uv = jmax(x - u, 0.0);
+    const bool fl = bits_finite(l), fu = bits_finite(u);
+    const double lv = pos_part(l - x), uv = pos_part(x - u);
     a[kN_LuSq] += lv * lv + uv * uv;
     a[kN_LuMax] = nan_max(a[kN_LuMax], nan_max(fabs(lv), fabs(uv)));
     a[kN_Cx] += c * x;
@@ -108,7 +127,7 @@ struct EvalN {
     a[kN_RcvMax] = nan_max(a[kN_RcvMax], fabs(rcv));
     a[kN_Contrib] += rc_contribution(rc, l, u);
     // primal ray, before division by ||x||_inf: bounds 0 where finite (:335-336)
-    const double lr = fl ? jmax(-x, 0.0) : 0.0, ur = fu ? jmax(x, 0.0) : 0.0;
+    const double lr = fl ? pos_part(-x) : 0.0, ur = fu ? pos_part(x) : 0.0;
     a[kN_RayLuMax] = nan_max(a[kN_RayLuMax], nan_max(lr, ur));
     // dual ray: objective set to zero, gradient - c (:346-354)
     const double gr = g - c;
@@ -136,11 +155,11 @@ struct EvalM {
     const double b = ob[i];
     const bool ineq = ineq_flag ? ineq_flag[i] != 0 : i >= neq;
     double cv = b - kx;                            // :26-45
-    if (ineq) cv = jmax(cv, 0.0);
+    if (ineq) cv = pos_part(cv);
     a[kM_CvSq] += cv * cv;
     a[kM_CvMax] = nan_max(a[kM_CvMax], fabs(cv));
     if (ineq) {
-      const double dr = jmax(-y, 0.0);             // :198-211
+      const double dr = pos_part(-y);             // :198-211
       a[kM_DrSq] += dr * dr;
       a[kM_DrMax] = nan_max(a[kM_DrMax], dr);
     }
@@ -148,7 +167,7 @@ struct EvalM {
     a[kM_YMax] = nan_max(a[kM_YMax], fabs(y));
     a[kM_YSq] += y * y;
     double cvr = -kx;                              // ray: right-hand side 0 (:338)
-    if (ineq) cvr = jmax(cvr, 0.0);
+    if (ineq) cvr = pos_part(cvr);
     a[kM_RayCvMax] = nan_max(a[kM_RayCvMax], fabs(cvr));
   }
 };
@@ -168,7 +187,7 @@ struct KktN {
   __device__ __forceinline__ void point(int p, const T* xs, const T* gs, long long j, double l, double u, double c,
                                         bool fl, bool fu, double* a) const {
     const double x = (double)xs[j], g = (double)gs[j];
-    const double lv = jmax(l - x, 0.0), uv = jmax(x - u, 0.0);
+    const double lv = pos_part(l - x), uv = pos_part(x - u);
     a[4 * p + 0] += lv * lv + uv * uv;
     a[4 * p + 1] += c * x;
     const double rc = reduced_cost(g, fl, fu);
@@ -178,7 +197,7 @@ struct KktN {
   }
   __device__ __forceinline__ void operator()(long long j, double* a) const {
     const double l = (double)this->l[j], u = (double)this->u[j], c = (double)this->c[j];
-    const bool fl = isfinite(l), fu = isfinite(u);
+    const bool fl = bits_finite(l), fu = bits_finite(u);
     point(0, x0, g0, j, l, u, c, fl, fu, a);
     point(1, x1, g1, j, l, u, c, fl, fu, a);
     point(2, x2, g2, j, l, u, c, fl, fu, a);
@@ -198,10 +217,10 @@ struct KktM {
                                         double* a) const {
     const double y = (double)ys[i], kx = (double)ks[i];
     double cv = b - kx;
-    if (ineq) cv = jmax(cv, 0.0);
+    if (ineq) cv = pos_part(cv);
     a[3 * p + 0] += cv * cv;
     if (ineq) {
-      const double dr = jmax(-y, 0.0);
+      const double dr = pos_part(-y);
       a[3 * p + 1] += dr * dr;
     }
     a[3 * p + 2] += b * y;
