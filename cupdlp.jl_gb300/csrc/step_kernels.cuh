@@ -153,13 +153,19 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_ke
       e.dx = lds(a.kty + j);
     }
   };
-  // x^ = proj(x - (tau/omega)(c - K'y)) and dx (:177-197); returns ||dx||^2 of the entry
-  auto candidate = [&](int j, T xv, T ktyv, const PrimalIn<T>& e) -> T {
+  // x^ = proj(x - (tau/omega)(c - K'y)) and dx (:177-197); its ||dx||^2 term goes into the
+  // CTA's sum with one FMA, or into the split row's own slot
+  auto candidate = [&](int j, T xv, T ktyv, const PrimalIn<T>& e, const Tile& t, bool split) {
     T v = xv - tto * (e.c - ktyv);
     v = imin(e.u, imax(e.l, v));   // min(u, max(l, .)) (:192)
     const T d = v - xv;
     a.dx[j] = direct ? v : d;      // gathered by the dual kernel next: a normal (L2-resident) store
-    return d * d;
+    if (split) {
+      a.part_p_split[t.split] = (double)(d * d);
+      __threadfence();
+    } else {
+      acc = fma(d, d, acc);
+    }
   };
   // split handling and the fused epilogue of tile t, once its row sums are in rs
   auto finish = [&](const Tile& t, const PrimalIn<T>& e) {
@@ -175,29 +181,13 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_ke
         sts(a.kty + j, ktyv);                       // K'y = A'y (:307)
         sts(a.sx + j, e.sx + xv * w);               // weighted sums (src/saddle_point_gpu.jl:137,182)
         sts(a.skty + j, e.sk + ktyv * w);
-        if (!commit_only) {
-          const T d2 = candidate(j, xv, ktyv, e);
-          if (split) {
-            a.part_p_split[t.split] = (double)d2;
-            __threadfence();
-          } else {
-            acc += d2;
-          }
-        }
+        if (!commit_only) candidate(j, xv, ktyv, e, t, split);
       }
       __syncwarp();
     } else {
       // previous attempt rejected: K'y is unchanged, only the candidate is recomputed
       const int rows = (split && t.piece != t.pieces - 1) ? 0 : t.rows;
-      if (lane < rows) {
-        const T d2 = candidate(j, e.x, e.dx, e);
-        if (split) {
-          a.part_p_split[t.split] = (double)d2;
-          __threadfence();
-        } else {
-          acc += d2;
-        }
-      }
+      if (lane < rows) candidate(j, e.x, e.dx, e, t, split);
     }
   };
   TileLoad<T> L0;
@@ -412,8 +402,8 @@ __global__ void __launch_bounds__(kBlock, 4) dual_step_kernel(DualArgs<T> a) {
         a.part_d_split[2 * t.split + 1] = (double)(d * d);
         __threadfence();
       } else {
-        acc_i += kdx * d;
-        acc_d += d * d;
+        acc_i = fma(kdx, d, acc_i);
+        acc_d = fma(d, d, acc_d);
       }
     }
     __syncwarp();
