@@ -126,8 +126,8 @@ struct Workspace {
     for (DBuf<T>* v : {&y0, &y1, &kx0, &kx1, &sy, &skx, &ay, &akx, &ry, &rkx, &tmp_m}) v->alloc(M);
     st_dev.alloc(1);
     CK(cudaMemsetAsync(st_dev.get(), 0, sizeof(StepState), s));
-    build_tile_plan(plan_p, P->At, {0, n}, {}, s);
-    build_tile_plan(plan_d, P->A, {0, m}, {P->neq}, s);
+    build_tile_plan(plan_p, P->At, {0, n}, {}, kPrimalCtasPerSm<T>, s);
+    build_tile_plan(plan_d, P->A, {0, m}, {P->neq}, kDualCtasPerSm, s);
     part_p.alloc(plan_p.num_ctas);
     part_d.alloc(2 * (size_t)plan_d.num_ctas);
     part_p_split.alloc(std::max(plan_p.num_splits, 1));

@@ -94,6 +94,47 @@ struct DualArgs {
   int direct;            // dx holds x^ and the row sums are K x^ (see above)
 };
 
+// Sums over the CTA of Q per-thread partials in a fixed order, valid in thread 0; `sh`
+// holds Q * kBlock doubles and may be reused by consecutive calls. FP64 partials go through
+// shared memory: lane l of warp 0 adds entry l of every warp in warp order, then one shuffle
+// tree finishes (12 warp-wide FP64 adds per quantity, where a shuffle tree in every warp
+// takes 40: GB300 issues FP64 at 2 lanes per SM and cycle). FP32 partials: a shuffle tree
+// per warp in FP32, the warp sums added in FP64.
+template <int Q, class T>
+__device__ __forceinline__ void cta_sums(const T (&v)[Q], double (&out)[Q], double* sh) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  __syncthreads();  // a previous call's readers are done with sh
+  if constexpr (sizeof(T) == 8) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) sh[q * kBlock + t] = v[q];
+    __syncthreads();
+    if (t < 32) {
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        double s = sh[q * kBlock + lane];
+#pragma unroll
+        for (int w = 1; w < kBlock / 32; ++w) s += sh[q * kBlock + w * 32 + lane];
+        out[q] = warp_sum(s);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const T ws = warp_sum(v[q]);
+      if (lane == 0) sh[q * 32 + warp] = (double)ws;
+    }
+    __syncthreads();
+    if (t == 0) {
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        double s = 0.0;
+        for (int w = 0; w < kBlock / 32; ++w) s += sh[q * 32 + w];
+        out[q] = s;
+      }
+    }
+  }
+}
+
 // One lane's epilogue inputs for its row of a tile (issued with the tile's matrix loads).
 template <class T>
 struct PrimalIn {
@@ -107,10 +148,10 @@ struct PrimalIn {
 };
 
 template <class T>
-__global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_kernel(PrimalArgs<T> a) {
+__global__ void __launch_bounds__(kBlock, kPrimalCtasPerSm<T>) primal_step_kernel(PrimalArgs<T> a) {
   __shared__ T rs_all[kBlock / 32][32];
-  __shared__ double wsum[kBlock / 32];
-  __shared__ T wpart[kBlock / 32];
+  __shared__ double red[kBlock];
+  __shared__ T wlane[kBlock];
   __shared__ Tile tl[kTilesPerCtaMax];
   const int b = a.plan.cta_map ? a.plan.cta_map[blockIdx.x] : (int)blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -200,7 +241,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_ke
     Tile t{};
     if (has) t = tl[q];
     if (has && sub == 0) load_in(t, E0);
-    if (pending) group_row_sum(a.At.col, a.At.val, yg, t, has, W, sub, wpart, rs);
+    if (pending) group_row_sum(a.At.col, a.At.val, yg, t, has, W, sub, wlane, rs);
     if (has && sub == 0) finish(t, E0);
   } else {
     // each warp walks its tiles q = warp, warp + 8, ...: a tile's epilogue inputs, row
@@ -216,14 +257,10 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) primal_step_ke
     }
   }
   if (commit_only) return;
-  const T ws = warp_sum(acc);
-  if (lane == 0) wsum[warp] = (double)ws;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double p = 0.0;
-    for (int k = 0; k < kBlock / 32; ++k) p += wsum[k];
-    a.part_p[b] = p;
-  }
+  const T v[1] = {acc};
+  double o[1];
+  cta_sums<1>(v, o, red);
+  if (threadIdx.x == 0) a.part_p[b] = o[0];
 }
 
 // Decision of take_step! for one attempt, on a copy of the instance's state (the caller
@@ -296,28 +333,6 @@ __device__ __forceinline__ void step_factors(const StepState& s, long long k, do
   }
 }
 
-// Sum of three values over the CTA in a fixed order (valid in thread 0); `sh` holds 3 x 32.
-__device__ __forceinline__ void block_sum3(double& a, double& b, double& c, double* sh) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  a = warp_sum(a);
-  b = warp_sum(b);
-  c = warp_sum(c);
-  if (lane == 0) {
-    sh[wid] = a;
-    sh[32 + wid] = b;
-    sh[64 + wid] = c;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    a = b = c = 0.0;
-    for (int w = 0; w < kBlock / 32; ++w) {
-      a += sh[w];
-      b += sh[32 + w];
-      c += sh[64 + w];
-    }
-  }
-}
-
 // One lane's epilogue inputs for its row of a tile of A (issued with the tile's matrix loads).
 template <class T>
 struct DualIn {
@@ -329,12 +344,11 @@ struct DualIn {
 };
 
 template <class T>
-__global__ void __launch_bounds__(kBlock, 4) dual_step_kernel(DualArgs<T> a) {
+__global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualArgs<T> a) {
   __shared__ T rs_all[kBlock / 32][32];
-  __shared__ double wsum[2][kBlock / 32];
-  __shared__ T wpart[kBlock / 32];
+  __shared__ T wlane[kBlock];
   __shared__ Tile tl[kTilesPerCtaMax];
-  __shared__ double red3[3 * 32];
+  __shared__ double red[2 * kBlock];
   __shared__ int is_last;
   const int b = a.plan.cta_map ? a.plan.cta_map[blockIdx.x] : (int)blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -417,7 +431,7 @@ __global__ void __launch_bounds__(kBlock, 4) dual_step_kernel(DualArgs<T> a) {
     Tile t{};
     if (has) t = tl[q];
     if (has && sub == 0) load_in(t, E0);
-    if (!commit_only) group_row_sum(a.A.col, a.A.val, a.dx, t, has, W, sub, wpart, rs);
+    if (!commit_only) group_row_sum(a.A.col, a.A.val, a.dx, t, has, W, sub, wlane, rs);
     if (has && sub == 0) finish(t, E0);
   } else {
     for (int q = warp; q < nt; q += kBlock / 32) {
@@ -430,33 +444,43 @@ __global__ void __launch_bounds__(kBlock, 4) dual_step_kernel(DualArgs<T> a) {
       finish(t, E0);
     }
   }
-  if (!commit_only) {
-    const T wi = warp_sum(acc_i), wd = warp_sum(acc_d);
-    if (lane == 0) {
-      wsum[0][warp] = (double)wi;
-      wsum[1][warp] = (double)wd;
-    }
-  }
-  __syncthreads();
   const int inst = a.plan.cta_inst[b];
   const int c0 = a.plan.inst_cta_begin[inst], c1 = a.plan.inst_cta_begin[inst + 1];
-  if (threadIdx.x == 0) {
-    if (!commit_only) {
-      double si = 0.0, sd = 0.0;
-      for (int k = 0; k < kBlock / 32; ++k) {
-        si += wsum[0][k];
-        sd += wsum[1][k];
-      }
-      a.part_d[b] = si;
-      a.part_d[a.plan.num_ctas + b] = sd;
+  StepState* stw = a.st_mut + inst;
+  if (!commit_only) {
+    const T v[2] = {acc_i, acc_d};
+    double o[2];
+    cta_sums<2>(v, o, red);
+    if (threadIdx.x == 0) {
+      a.part_d[b] = o[0];
+      a.part_d[a.plan.num_ctas + b] = o[1];
     }
+    if (b == c0) {
+      // the instance's primal ||dx||^2 in plan order (CTAs, then split rows), summed here
+      // once so that the deciding CTA reads one value instead of every primal partial
+      const int p0 = a.p_cta_begin[inst], p1 = a.p_cta_begin[inst + 1];
+      const int q0 = a.p_split_begin[inst], q1 = a.p_split_begin[inst + 1];
+      double sx[1] = {0.0};
+      for (int k0 = p0 + (int)threadIdx.x; k0 < p1; k0 += 4 * kBlock) {
+        double u[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) u[j] = k0 + j * kBlock < p1 ? __ldcg(a.part_p + k0 + j * kBlock) : 0.0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) sx[0] += u[j];
+      }
+      for (int k = q0 + (int)threadIdx.x; k < q1; k += kBlock) sx[0] += __ldcg(a.part_p_split + k);
+      double ox[1];
+      cta_sums<1>(sx, ox, red);
+      if (threadIdx.x == 0) stw->dx2_sum = ox[0];
+    }
+  }
+  if (threadIdx.x == 0) {
     __threadfence();
-    const unsigned prev = atomicAdd(&a.st_mut[inst].arrive, 1u);
+    const unsigned prev = atomicAdd(&stw->arrive, 1u);
     is_last = (prev == (unsigned)(c1 - c0 - 1)) ? 1 : 0;
   }
   __syncthreads();
   if (!is_last) return;
-  StepState* stw = a.st_mut + inst;
   if (commit_only) {
     if (threadIdx.x == 0) {
       stw->pending_commit = 0;
@@ -464,50 +488,45 @@ __global__ void __launch_bounds__(kBlock, 4) dual_step_kernel(DualArgs<T> a) {
     }
     return;
   }
-  // the instance's last CTA: thread 0 fetches the state and the step-size factors first, so
-  // those loads overlap the partial reductions; partials in a fixed order
+  // the instance's last CTA: thread 0 fetches the state, the primal norm and the step-size
+  // factors first, so those loads overlap the partials' loads; partials in a fixed order
   __shared__ StepState s;
-  double f1 = 0.0, f2 = 0.0;
+  double f1 = 0.0, f2 = 0.0, dx2 = 0.0;
   if (threadIdx.x == 0) {
+    __threadfence();
     s = *stw;
+    dx2 = __ldcg(&stw->dx2_sum);
     step_factors(s, s.total_iters + (s.constant_step ? 0 : 1), f1, f2);
   }
-  // one round of loads for the three CTA ranges (dual interaction, dual ||dy||^2, primal
-  // ||dx||^2), all issued before any is added; split-row slots (rare) follow
-  constexpr int U = 4;
+  // one round of loads for both CTA ranges (interaction, ||dy||^2) up to 4 x kBlock CTAs,
+  // all issued before any is added; split-row slots (rare) follow
   const int s0 = a.plan.inst_split_begin[inst], s1 = a.plan.inst_split_begin[inst + 1];
-  const int p0 = a.p_cta_begin[inst], p1 = a.p_cta_begin[inst + 1];
-  const int q0 = a.p_split_begin[inst], q1 = a.p_split_begin[inst + 1];
-  const int span = max(c1 - c0, p1 - p0);
-  double si = 0.0, sd = 0.0, sx = 0.0;
-  for (int k0 = (int)threadIdx.x; k0 < span; k0 += U * kBlock) {
-    double vi[U], vd[U], vx[U];
+  double sd[2] = {0.0, 0.0};
+  for (int k0 = c0 + (int)threadIdx.x; k0 < c1; k0 += 4 * kBlock) {
+    double ui[4], ud[4];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int k = k0 + u * kBlock;
-      const bool ind = c0 + k < c1, inp = p0 + k < p1;
-      vi[u] = ind ? __ldcg(a.part_d + c0 + k) : 0.0;
-      vd[u] = ind ? __ldcg(a.part_d + a.plan.num_ctas + c0 + k) : 0.0;
-      vx[u] = inp ? __ldcg(a.part_p + p0 + k) : 0.0;
+    for (int j = 0; j < 4; ++j) {
+      const bool in = k0 + j * kBlock < c1;
+      ui[j] = in ? __ldcg(a.part_d + k0 + j * kBlock) : 0.0;
+      ud[j] = in ? __ldcg(a.part_d + a.plan.num_ctas + k0 + j * kBlock) : 0.0;
     }
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      si += vi[u];
-      sd += vd[u];
-      sx += vx[u];
+    for (int j = 0; j < 4; ++j) {
+      sd[0] += ui[j];
+      sd[1] += ud[j];
     }
   }
-  for (int k = s0 + threadIdx.x; k < s1; k += kBlock) {
-    si += __ldcg(a.part_d_split + 2 * k);
-    sd += __ldcg(a.part_d_split + 2 * k + 1);
+  for (int k = s0 + (int)threadIdx.x; k < s1; k += kBlock) {
+    sd[0] += __ldcg(a.part_d_split + 2 * k);
+    sd[1] += __ldcg(a.part_d_split + 2 * k + 1);
   }
-  for (int k = q0 + threadIdx.x; k < q1; k += kBlock) sx += __ldcg(a.part_p_split + k);
-  block_sum3(si, sd, sx, red3);
+  double tot[2];
+  cta_sums<2>(sd, tot, red);
   if (threadIdx.x == 0) {
     s.arrive = 0;
     if (pending) s.primal_spmv += 1;
     s.pending_commit = 0;
-    step_decision(s, f1, f2, si, sx, sd);
+    step_decision(s, f1, f2, tot[0], dx2, tot[1]);
     *stw = s;
   }
 }

@@ -34,23 +34,21 @@ __device__ __forceinline__ void tile_load(const int32_t* __restrict__ row_ptr, c
   }
 }
 
-// Row sums of tile t from its loads: rs[r] = sum of val * xg[col] over row t.row_begin + r,
-// r < t.rows (a long-row tile, e_log2 < 0, goes to long_row_sum). Lane l owns the tile's nonzeros [l E, (l + 1) E), E = 2^e_log2: it gathers
-// their entries of xg (all in flight together) and sums them per row with one FMA per
-// nonzero. The row offsets are read from the lanes' registers with shuffles; a row that
-// crosses lanes is completed by a segmented shuffle scan of the lanes' trailing partial
-// sums. Every sum's order depends only on the tile, never on its position in memory. rs
-// (32 entries per warp) is complete after the final __syncwarp.
 // A warp's rounds r0, r0 + step, ... (< nnz) of a long row: 32 x kLongRound coalesced
-// (column, value) loads per round, all issued before the round's gathers, FMAs into four
-// independent accumulators. Returns the lane's sum (fixed order: accumulators added
-// pairwise). (Keeping two rounds in flight needed more registers than the kernels' occupancy
-// leaves and measured slower.)
+// (column, value) loads per round, all issued before the round's gathers, then one FMA per
+// nonzero. FP32 keeps four independent accumulators (added pairwise at the end); FP64 keeps
+// one: its FMAs issue at 2 lanes per SM and cycle, so a dependent chain costs no throughput
+// and the three combining adds would. Returns the lane's sum (fixed order). (Keeping two
+// rounds in flight needed more registers than the kernels' occupancy leaves and measured
+// slower.)
 template <class T>
 __device__ __forceinline__ T stream_rounds(const int32_t* __restrict__ cp, const T* __restrict__ vp,
                                            const T* __restrict__ xg, int nnz, int r0, int step) {
+  constexpr int kAcc = sizeof(T) == 8 ? 1 : 4;
   const int lane = threadIdx.x & 31;
-  T acc[4] = {T(0), T(0), T(0), T(0)};
+  T acc[kAcc];
+#pragma unroll
+  for (int j = 0; j < kAcc; ++j) acc[j] = T(0);
   for (; r0 < nnz; r0 += step) {
     int c[kLongRound];
     T v[kLongRound];
@@ -62,9 +60,10 @@ __device__ __forceinline__ T stream_rounds(const int32_t* __restrict__ cp, const
     }
 #pragma unroll
     for (int j = 0; j < kLongRound; ++j)
-      if (r0 + j * 32 + lane < nnz) acc[j & 3] = fma(v[j], xg[c[j]], acc[j & 3]);
+      if (r0 + j * 32 + lane < nnz) acc[j % kAcc] = fma(v[j], xg[c[j]], acc[j % kAcc]);
   }
-  return (acc[0] + acc[1]) + (acc[2] + acc[3]);
+  if constexpr (kAcc == 1) return acc[0];
+  else return (acc[0] + acc[1]) + (acc[2] + acc[3]);
 }
 
 // One row of up to kWarpShare nonzeros summed by the whole warp (valid in lane 0).
@@ -75,29 +74,39 @@ __device__ __forceinline__ T long_row_sum(const int32_t* __restrict__ col, const
 }
 
 // Group tiles: the CTA's warps form groups of W = 2^g; group q sums tile q's row (or piece),
-// warp `sub` of the group streaming rounds sub, sub + W, ..., and the group's sums are added
-// in warp order. Every thread must call it (warps without a tile pass has = false); the row's
-// sum is in rs[0] of the group's first warp after the final __syncwarp.
+// warp `sub` of the group streaming rounds sub, sub + W, ... The lanes' sums meet in shared
+// memory (wlane, 32 per warp): lane l of the group's first warp adds lane l of each warp in
+// warp order, and one shuffle tree finishes the row (W - 1 + 5 warp-wide adds instead of a
+// shuffle tree per warp). Every thread must call it (warps without a tile pass has = false);
+// the row's sum is in rs[0] of the group's first warp after the final __syncwarp.
 template <class T>
 __device__ __forceinline__ void group_row_sum(const int32_t* __restrict__ col, const T* __restrict__ val,
                                               const T* __restrict__ xg, const Tile& t, bool has, int W, int sub,
-                                              T* wpart, T* rs) {
+                                              T* wlane, T* rs) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   T part = T(0);
   if (has)
     part = stream_rounds(col + t.nnz_begin, val + t.nnz_begin, xg, t.nnz, sub * 32 * kLongRound,
                          W * 32 * kLongRound);
-  const T ws = warp_sum(part);
-  if (lane == 0) wpart[warp] = ws;
+  wlane[threadIdx.x] = part;
   __syncthreads();
-  if (has && sub == 0 && lane == 0) {
-    T s = T(0);
-    for (int w = 0; w < W; ++w) s += wpart[warp + w];
-    rs[0] = s;
+  if (has && sub == 0) {
+    T s = part;
+    for (int w = 1; w < W; ++w) s += wlane[(warp + w) * 32 + lane];
+    s = warp_sum(s);
+    if (lane == 0) rs[0] = s;
   }
   __syncwarp();
 }
 
+// Row sums of tile t from its loads: rs[r] = sum of val * xg[col] over row t.row_begin + r,
+// r < t.rows (a long-row tile, e_log2 < 0, goes to long_row_sum). Lane l owns the tile's
+// nonzeros [l E, (l + 1) E), E = 2^e_log2: it gathers
+// their entries of xg (all in flight together) and sums them per row with one FMA per
+// nonzero. The row offsets are read from the lanes' registers with shuffles; a row that
+// crosses lanes is completed by a segmented shuffle scan of the lanes' trailing partial
+// sums. Every sum's order depends only on the tile, never on its position in memory. rs
+// (32 entries per warp) is complete after the final __syncwarp.
 template <class T>
 __device__ __forceinline__ void tile_sums(const int32_t* __restrict__ col, const T* __restrict__ val,
                                           const T* __restrict__ xg, const Tile& t, const TileLoad<T>& L, T* rs) {

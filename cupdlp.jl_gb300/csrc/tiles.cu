@@ -76,7 +76,7 @@ void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t
 
 template <class T>
 void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector<int32_t>& bounds,
-                     const std::vector<int32_t>& aux, cudaStream_t s) {
+                     const std::vector<int32_t>& aux, int ctas_per_sm, cudaStream_t s) {
   if ((int32_t)M.host_rp.size() != M.nrows + 1) throw Error(GPDHG_ERR_INTERNAL, "matrix has no host row pointer");
   const int K = (int)bounds.size() - 1;
   std::vector<Tile> tiles;
@@ -89,10 +89,12 @@ void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector
     list_tiles(M.host_rp.data(), bounds[k], bounds[k + 1], k, aux.empty() ? 0 : aux[k], TileTraits<T>::kNnz,
                TileTraits<T>::kEMax, tiles, splits, carries);
     // CTAs: 8 / W group tiles of one width W together; other consecutive tiles of this
-    // instance in groups of tpc, where tpc grows from 8 to 32 once the instance has more than
-    // ~1,200 tiles (8 CTAs per SM of 152)
+    // instance in groups of tpc: 8 while the instance has fewer tiles than one per warp of
+    // every resident CTA slot (152 SMs x ctas_per_sm), then as many as make the instance's
+    // CTAs one wave, up to kTilesPerCtaMax
     const long long nt = (long long)(tiles.size() - t0);
-    const long long tpc = std::min<long long>(kTilesPerCtaMax, std::max<long long>(kTilesPerCtaMin, (nt + 1215) / 1216));
+    const long long slots = 152LL * ctas_per_sm;
+    const long long tpc = std::min<long long>(kTilesPerCtaMax, std::max<long long>(kTilesPerCtaMin, (nt + slots - 1) / slots));
     long long open = 0;   // tiles in the CTA being filled
     int open_code = 0;    // its tiles' kind: 0 normal, else the group code
     for (size_t q = t0; q < tiles.size(); ++q) {
@@ -132,8 +134,8 @@ void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector
 }
 
 template void build_tile_plan<float>(TilePlan<float>&, const DeviceMatrix&, const std::vector<int32_t>&,
-                                     const std::vector<int32_t>&, cudaStream_t);
+                                     const std::vector<int32_t>&, int, cudaStream_t);
 template void build_tile_plan<double>(TilePlan<double>&, const DeviceMatrix&, const std::vector<int32_t>&,
-                                      const std::vector<int32_t>&, cudaStream_t);
+                                      const std::vector<int32_t>&, int, cudaStream_t);
 
 }  // namespace gpdhg

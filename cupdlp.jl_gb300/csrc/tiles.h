@@ -6,12 +6,12 @@
 // warps (about kWarpShare nonzeros each) split it and combine their sums in shared memory,
 // 8 / W such rows to a CTA; a row longer than kCtaNnz is cut into 8-warp pieces of kCtaNnz
 // whose partial sums meet in a carry array. Consecutive tiles of one instance form a CTA's
-// work (8 to 32 tiles, dealt to its 8 warps in turn, or 8 / W group tiles), so every CTA
+// work (8 to 96 tiles, dealt to its 8 warps in turn, or 8 / W group tiles), so every CTA
 // belongs to exactly one instance and the per-instance step decision can count CTAs. An
-// instance with few tiles gets one tile per warp (most CTAs in flight), a large one up to
-// four per warp (fewer partial sums for the step decision to reduce). The decomposition
-// depends only on the instance's own row lengths, never on where the instance sits in a
-// packed batch.
+// instance with few tiles gets one tile per warp (most CTAs in flight), a large one as many
+// as make its CTAs a single wave over the GPU (no ragged last wave, and fewer partial sums
+// for the step decision to reduce). The decomposition depends only on the instance's own
+// row lengths, never on where the instance sits in a packed batch.
 #pragma once
 
 #include <vector>
@@ -32,7 +32,13 @@ constexpr int kWarpShare = 512;   // nonzeros per warp of a long row
 constexpr int kCtaNnz = 16384;    // longest row (piece) one CTA sums
 constexpr int kLongRound = 8;     // (column, value) loads per lane and round of a long row
 constexpr int kTilesPerCtaMin = 8;   // tiles per CTA: one per warp for small instances,
-constexpr int kTilesPerCtaMax = 32;  // up to four per warp for large ones
+constexpr int kTilesPerCtaMax = 96;  // up to twelve per warp for large ones
+// Resident CTAs per SM of the step kernels (their __launch_bounds__ minimum): a large
+// instance gets one CTA per resident slot of the GPU's 152 SMs, so its CTAs run as one wave
+// with no partly filled last wave.
+template <class T>
+constexpr int kPrimalCtasPerSm = sizeof(T) == 8 ? 3 : 4;
+constexpr int kDualCtasPerSm = 4;
 
 constexpr int kWarpLong = -1;  // Tile::e_log2 of a row streamed by one warp
 // Tile::e_log2 of a row summed by 2^g warps (g = 1, 2, 3)
@@ -92,6 +98,6 @@ void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t
 // aux[k], or 0 when aux is empty).
 template <class T>
 void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector<int32_t>& bounds,
-                     const std::vector<int32_t>& aux, cudaStream_t s);
+                     const std::vector<int32_t>& aux, int ctas_per_sm, cudaStream_t s);
 
 }  // namespace gpdhg

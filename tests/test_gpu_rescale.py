@@ -52,7 +52,10 @@ def test_device_rescaled_solve_reaches_the_same_optimum():
     assert r_dev.termination_reason == r_host.termination_reason == 1
     ph = r_host.last_iteration_stats.convergence_information.primal_objective
     pd = r_dev.last_iteration_stats.convergence_information.primal_objective
-    assert pd == pytest.approx(ph, rel=1e-8)
+    # the two scaled problems differ at round-off level (Pock-Chambolle sums in another
+    # order), so the two runs take different paths and each stops somewhere inside the
+    # 1e-8 relative-KKT ball around the optimum
+    assert pd == pytest.approx(ph, rel=1e-7)
     assert pd == pytest.approx(lp.optimal_objective, rel=1e-6)
     # the unscaled solution of the device path satisfies the bounds
     xu = x / var
