@@ -95,8 +95,9 @@ struct StepState {
   long long primal_spmv;   // attempts whose primal kernel also ran A'y (a commit)
   const double* pow_table; // [1-(k+1)^-r, 1+(k+1)^-g] for k < pow_table_len (device)
   long long pow_table_len;
-  double dx2_sum;          // this attempt's primal ||dx||^2, summed in plan order by the
-                           // instance's first dual CTA for the deciding CTA (read from L2)
+  // written in every attempt by the instance's first dual CTA, for the deciding CTA:
+  double half_w_dx2;       // 0.5 * omega * ||dx|| * ||dx||: the primal part of the movement
+  double f1, f2;           // step-size factors for this attempt's counter
 };
 
 // ----------------------------------------------------------------------------------

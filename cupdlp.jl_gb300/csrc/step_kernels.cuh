@@ -263,10 +263,18 @@ __global__ void __launch_bounds__(kBlock, kPrimalCtasPerSm<T>) primal_step_kerne
   if (threadIdx.x == 0) a.part_p[b] = o[0];
 }
 
+// Primal part of take_step!'s movement (:324-333), 0.5 * omega * ||dx||^2 evaluated as the
+// reference does (the norm squared again).
+__device__ __forceinline__ double half_w_dx2(double omega, double dx2) {
+  const double ndx = sqrt(dx2);
+  return 0.5 * omega * ndx * ndx;
+}
+
 // Decision of take_step! for one attempt, on a copy of the instance's state (the caller
 // writes it back). f1 / f2 are the step-size factors (1 - (k+1)^-r), (1 + (k+1)^-g)
-// for the attempt counter after this attempt, fetched early by the caller (host table).
-__device__ __forceinline__ void step_decision(StepState& s, double f1, double f2, double inter_signed, double dx2,
+// for the attempt counter after this attempt and hw_dx2 = half_w_dx2(omega, ||dx||^2),
+// all prepared by the instance's first dual CTA while the others still run.
+__device__ __forceinline__ void step_decision(StepState& s, double f1, double f2, double inter_signed, double hw_dx2,
                                               double dy2) {
   s.total_iters += s.constant_step ? 0 : 1;
   s.kkt_passes += 1.0;
@@ -274,8 +282,8 @@ __device__ __forceinline__ void step_decision(StepState& s, double f1, double f2
   const double omega = s.omega;
   const double tau = s.tau;
   const double inter = fabs(inter_signed);
-  const double ndx = sqrt(dx2), ndy = sqrt(dy2);
-  const double movement = 0.5 * omega * ndx * ndx + (0.5 / omega) * ndy * ndy;
+  const double ndy = sqrt(dy2);
+  const double movement = hw_dx2 + (0.5 / omega) * ndy * ndy;
   double limit;
   bool accept;
   if (s.constant_step) {
@@ -471,7 +479,14 @@ __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualA
       for (int k = q0 + (int)threadIdx.x; k < q1; k += kBlock) sx[0] += __ldcg(a.part_p_split + k);
       double ox[1];
       cta_sums<1>(sx, ox, red);
-      if (threadIdx.x == 0) stw->dx2_sum = ox[0];
+      if (threadIdx.x == 0) {
+        // and the decision's other inputs that need no dual partial
+        double f1, f2;
+        step_factors(*st, st->total_iters + (st->constant_step ? 0 : 1), f1, f2);
+        stw->half_w_dx2 = half_w_dx2(st->omega, ox[0]);
+        stw->f1 = f1;
+        stw->f2 = f2;
+      }
     }
   }
   if (threadIdx.x == 0) {
@@ -488,16 +503,14 @@ __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualA
     }
     return;
   }
-  // the instance's last CTA: thread 0 fetches the state, the primal norm and the step-size
-  // factors first, so those loads overlap the partials' loads; partials in a fixed order
+  // the instance's last CTA: the first threads copy the state from L2 (the first CTA's
+  // fields are not in this SM's L1), one 8-byte word each, with the partials' loads; the
+  // barriers of cta_sums order the copy before thread 0 uses it. Partials in a fixed order.
   __shared__ StepState s;
-  double f1 = 0.0, f2 = 0.0, dx2 = 0.0;
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s = *stw;
-    dx2 = __ldcg(&stw->dx2_sum);
-    step_factors(s, s.total_iters + (s.constant_step ? 0 : 1), f1, f2);
-  }
+  static_assert(sizeof(StepState) % 8 == 0 && sizeof(StepState) / 8 <= kBlock, "StepState copy");
+  if (threadIdx.x < sizeof(StepState) / 8)
+    reinterpret_cast<unsigned long long*>(&s)[threadIdx.x] =
+        __ldcg(reinterpret_cast<const unsigned long long*>(stw) + threadIdx.x);
   // one round of loads for both CTA ranges (interaction, ||dy||^2) up to 4 x kBlock CTAs,
   // all issued before any is added; split-row slots (rare) follow
   const int s0 = a.plan.inst_split_begin[inst], s1 = a.plan.inst_split_begin[inst + 1];
@@ -526,7 +539,7 @@ __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualA
     s.arrive = 0;
     if (pending) s.primal_spmv += 1;
     s.pending_commit = 0;
-    step_decision(s, f1, f2, tot[0], dx2, tot[1]);
+    step_decision(s, s.f1, s.f2, tot[0], s.half_w_dx2, tot[1]);
     *stw = s;
   }
 }

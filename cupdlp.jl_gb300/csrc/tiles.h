@@ -37,7 +37,7 @@ constexpr int kTilesPerCtaMax = 96;  // up to twelve per warp for large ones
 // instance gets one CTA per resident slot of the GPU's 152 SMs, so its CTAs run as one wave
 // with no partly filled last wave.
 template <class T>
-constexpr int kPrimalCtasPerSm = sizeof(T) == 8 ? 3 : 4;
+constexpr int kPrimalCtasPerSm = sizeof(T) == 8 ? 4 : 4;
 constexpr int kDualCtasPerSm = 4;
 
 constexpr int kWarpLong = -1;  // Tile::e_log2 of a row streamed by one warp
