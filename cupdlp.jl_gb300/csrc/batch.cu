@@ -203,6 +203,7 @@ struct BatchWorkspace {
   DBuf<StepState> st_dev;
   PinnedBuf<StepState> st_host;
   DBuf<double> part_p, part_d, red_part, red_out;
+  DBuf<double> rvar, rcon;   // 1 / variable and 1 / constraint rescaling (evaluation divisions)
   PinnedBuf<double> red_host;
   TilePlan<T> plan_p, plan_d;   // tiles of the packed A' and A, instance by instance
   DBuf<double> part_p_split, part_d_split;
@@ -252,6 +253,10 @@ struct BatchWorkspace {
     }
     alloc_all<T>({&x, &dx, &kty, &sx, &skty, &ax, &agrad, &grad, &rx, &rgrad}, N);
     alloc_all<T>({&y0, &y1, &kx0, &kx1, &sy, &skx, &ay, &akx, &ry, &rkx}, M);
+    rvar.alloc(std::max(N, 1));
+    rcon.alloc(std::max(M, 1));
+    launch_reciprocal(B->var.get(), rvar.get(), N, s);
+    launch_reciprocal(B->con.get(), rcon.get(), M, s);
     st_dev.alloc(count);
     CK(cudaMemsetAsync(st_dev.get(), 0, sizeof(StepState) * count, s));
     build_tile_plan(plan_p, B->At, B->col_off, {}, kPrimalCtasPerSm<T>, s);
@@ -437,6 +442,10 @@ static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& 
       if (!retired[k] && due[k]) {
         fh[k] = 1;
         fh[K + k] = (st[k].numerical_error || st[k].count_primal == 0 || st[k].count_dual == 0) ? 1 : 0;
+        if (!fh[K + k]) {
+          st[k].rcp_w_primal = 1.0 / st[k].sum_w_primal;
+          st[k].rcp_w_dual = 1.0 / st[k].sum_w_dual;
+        }
         st[k].kkt_passes += 2.0;
         st[k].done = 0;
         any = true;
@@ -462,9 +471,11 @@ static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& 
       }
       W.launches += 2;
       W.template seg_reduce<kEvalNQ, kEvalNMax>(
-          true, EvalN<T>{W.ax.get(), W.agrad.get(), B->var.get(), B->ol.get(), B->ou.get(), B->oc.get()}, 0);
+          true, EvalN<T>{W.ax.get(), W.agrad.get(), B->var.get(), W.rvar.get(), B->ol.get(), B->ou.get(), B->oc.get()},
+          0);
       W.template seg_reduce<kEvalMQ, kEvalMMax>(
-          false, EvalM<T>{W.ay.get(), W.akx.get(), B->con.get(), B->ob.get(), 0, B->ineq_flag.get()}, 16);
+          false, EvalM<T>{W.ay.get(), W.akx.get(), B->con.get(), W.rcon.get(), B->ob.get(), 0, B->ineq_flag.get()},
+          16);
       W.fetch();
       bool any_restart_check = false;
       std::vector<char> check(K, 0);

@@ -20,14 +20,15 @@ namespace gpdhg {
 template <int Q, unsigned MAXMASK, class F>
 __global__ void __launch_bounds__(kBlock) seg_reduce_kernel(const SegItem* items, const uint8_t* active, F f,
                                                             double* partials, int num_items) {
-  __shared__ double sh[Q][kBlock / 32];
+  __shared__ double sh[Q * kBlock];
+  __shared__ double res[Q];
   const SegItem it = items[blockIdx.x];
   if (!active[it.inst]) return;
   double acc[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) acc[q] = 0.0;
   for (int i = it.begin + threadIdx.x; i < it.end; i += kBlock) f((long long)i, acc);
-  const double r = block_reduce_q<Q, MAXMASK>(acc, sh);
+  const double r = block_reduce_q<Q, MAXMASK>(acc, sh, res);
   if ((int)threadIdx.x < Q) partials[(size_t)threadIdx.x * num_items + blockIdx.x] = r;
 }
 
@@ -35,7 +36,8 @@ template <int Q, unsigned MAXMASK>
 __global__ void __launch_bounds__(kBlock) seg_finalize_kernel(const int32_t* inst_item_begin, const uint8_t* active,
                                                               const double* partials, int num_items, double* out,
                                                               int out_stride) {
-  __shared__ double sh[Q][kBlock / 32];
+  __shared__ double sh[Q * kBlock];
+  __shared__ double res[Q];
   const int inst = blockIdx.x;
   if (!active[inst]) return;
   const int k0 = inst_item_begin[inst], k1 = inst_item_begin[inst + 1];
@@ -49,7 +51,7 @@ __global__ void __launch_bounds__(kBlock) seg_finalize_kernel(const int32_t* ins
       acc[q] = ((MAXMASK >> q) & 1u) ? nan_max(acc[q], v) : acc[q] + v;
     }
   }
-  const double r = block_reduce_q<Q, MAXMASK>(acc, sh);
+  const double r = block_reduce_q<Q, MAXMASK>(acc, sh, res);
   if ((int)threadIdx.x < Q) out[(size_t)inst * out_stride + threadIdx.x] = r;
 }
 
@@ -73,9 +75,9 @@ __global__ void batch_average_n_kernel(BatchVecArgs<T> v, const uint8_t* use_cur
       ax[j] = x[j];
       agrad[j] = grad[j];
     } else {
-      const double wx = v.st[k].sum_w_primal, wy = v.st[k].sum_w_dual;
-      ax[j] = (T)((double)sx[j] / wx);
-      const T g = (T)(-(double)skty[j] / wy);
+      const StepState& q = v.st[k];
+      ax[j] = (T)div_rcp((double)sx[j], q.sum_w_primal, q.rcp_w_primal);
+      const T g = (T)(-div_rcp((double)skty[j], q.sum_w_dual, q.rcp_w_dual));
       agrad[j] = g + c[j];
     }
   }
@@ -92,9 +94,9 @@ __global__ void batch_average_m_kernel(BatchVecArgs<T> v, const uint8_t* use_cur
       ay[i] = p ? y1[i] : y0[i];
       akx[i] = p ? kx1[i] : kx0[i];
     } else {
-      const double wx = v.st[k].sum_w_primal, wy = v.st[k].sum_w_dual;
-      ay[i] = (T)((double)sy[i] / wy);
-      akx[i] = (T)((double)skx[i] / wx);
+      const StepState& q = v.st[k];
+      ay[i] = (T)div_rcp((double)sy[i], q.sum_w_dual, q.rcp_w_dual);
+      akx[i] = (T)div_rcp((double)skx[i], q.sum_w_primal, q.rcp_w_primal);
     }
   }
 }

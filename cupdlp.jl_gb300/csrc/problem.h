@@ -132,6 +132,8 @@ void validate_lp_desc(const gpdhg_lp_desc* d);
 void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d);
 // dst[k] = (float)src[k] on stream s.
 void launch_convert_d2f(const double* src, float* dst, long long n, cudaStream_t s);
+// dst[k] = 1 / src[k] on stream s.
+void launch_reciprocal(const double* src, double* dst, long long n, cudaStream_t s);
 // Ensures FP32 copies of the matrix values exist.
 void ensure_fp32_values(gpdhg_problem* p);
 // rescale_problem on the device (rescale.cu): rescales a problem built from an unscaled

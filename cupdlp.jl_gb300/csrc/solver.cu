@@ -38,6 +38,18 @@ void launch_convert_d2f(const double* src, float* dst, long long n, cudaStream_t
   CK_LAUNCH();
 }
 
+__global__ void reciprocal_kernel(long long len, const double* src, double* dst) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = 1.0 / src[i];
+}
+
+void launch_reciprocal(const double* src, double* dst, long long n, cudaStream_t s) {
+  if (n <= 0) return;
+  const int grid = std::max(1, std::min(ceil_div(n, kBlock), 4096));
+  reciprocal_kernel<<<grid, kBlock, 0, s>>>(n, src, dst);
+  CK_LAUNCH();
+}
+
 // Plain y = M x (warm start, power method, FP64 hand-off).
 struct NoPre {};
 template <class T>
@@ -88,6 +100,7 @@ struct Workspace {
   DBuf<StepState> st_dev;
   PinnedBuf<StepState> st_host;
   DBuf<double> part_p, part_d, red_part, red_out;
+  DBuf<double> rvar, rcon;   // 1 / variable and 1 / constraint rescaling (evaluation divisions)
   PinnedBuf<double> red_host;
   // segmented reductions over [0, n) and [0, m): the same layout a batch uses per instance
   DBuf<SegItem> seg_n, seg_m;
@@ -124,6 +137,10 @@ struct Workspace {
     }
     for (DBuf<T>* v : {&x, &dx, &kty, &sx, &skty, &ax, &agrad, &grad, &rx, &rgrad, &tmp_n}) v->alloc(N);
     for (DBuf<T>* v : {&y0, &y1, &kx0, &kx1, &sy, &skx, &ay, &akx, &ry, &rkx, &tmp_m}) v->alloc(M);
+    rvar.alloc(N);
+    rcon.alloc(M);
+    launch_reciprocal(P->var.get(), rvar.get(), n, s);
+    launch_reciprocal(P->con.get(), rcon.get(), m, s);
     st_dev.alloc(1);
     CK(cudaMemsetAsync(st_dev.get(), 0, sizeof(StepState), s));
     build_tile_plan(plan_p, P->At, {0, n}, {}, kPrimalCtasPerSm<T>, s);
@@ -346,22 +363,23 @@ bool run_phase(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopS
           CK(cudaMemcpyAsync(W.akx.get(), W.kxcur(p), sizeof(T) * m, cudaMemcpyDeviceToDevice, s));
         }
       } else {
+        const double rwx = 1.0 / st.sum_w_primal, rwy = 1.0 / st.sum_w_dual;
         average_n_kernel<T><<<gn, kBlock, 0, s>>>(n, W.sx.get(), W.skty.get(), W.c, st.sum_w_primal, st.sum_w_dual,
-                                                  W.ax.get(), W.agrad.get());
+                                                  rwx, rwy, W.ax.get(), W.agrad.get());
         CK_LAUNCH();
         ++P->launches;
         if (m) {
           average_m_kernel<T><<<gm, kBlock, 0, s>>>(m, W.sy.get(), W.skx.get(), st.sum_w_primal, st.sum_w_dual,
-                                                    W.ay.get(), W.akx.get());
+                                                    rwx, rwy, W.ay.get(), W.akx.get());
           CK_LAUNCH();
           ++P->launches;
         }
       }
       // unscaled statistics of the average, src/iteration_stats_utils_gpu.jl:447-502
-      W.template reduce<kEvalNQ, kEvalNMax>(true, EvalN<T>{W.ax.get(), W.agrad.get(), P->var.get(), P->ol.get(),
-                                                         P->ou.get(), P->oc.get()}, 0);
-      W.template reduce<kEvalMQ, kEvalMMax>(false, EvalM<T>{W.ay.get(), W.akx.get(), P->con.get(), P->ob.get(), P->neq, nullptr},
-                                            16);
+      W.template reduce<kEvalNQ, kEvalNMax>(true, EvalN<T>{W.ax.get(), W.agrad.get(), P->var.get(), W.rvar.get(),
+                                                         P->ol.get(), P->ou.get(), P->oc.get()}, 0);
+      W.template reduce<kEvalMQ, kEvalMMax>(false, EvalM<T>{W.ay.get(), W.akx.get(), P->con.get(), W.rcon.get(),
+                                                         P->ob.get(), P->neq, nullptr}, 16);
       W.fetch_reductions(16 + kEvalMQ);
       gpdhg_iteration_stats stats;
       std::memset(&stats, 0, sizeof(stats));

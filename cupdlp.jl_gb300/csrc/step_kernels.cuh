@@ -355,6 +355,7 @@ template <class T>
 __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualArgs<T> a) {
   __shared__ T rs_all[kBlock / 32][32];
   __shared__ T wlane[kBlock];
+  __shared__ T ipart[kBlock / 32][kBlock / 32];
   __shared__ Tile tl[kTilesPerCtaMax];
   __shared__ double red[2 * kBlock];
   __shared__ int is_last;
@@ -432,7 +433,15 @@ __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualA
   };
   TileLoad<T> L0;
   DualIn<T> E0;
-  if (nt > 0 && tl[0].e_log2 <= group_code(1)) {
+  bool interleave = nt == kBlock / 32;
+  for (int q = 0; q < nt && interleave; ++q) interleave = tl[q].e_log2 == kWarpLong;
+  if (interleave) {
+    // kBlock / 32 warp-streamed rows summed together (interleaved_rows_sum); warp w then
+    // finishes row w as if it had streamed it
+    load_in(tl[warp], E0);
+    if (!commit_only) interleaved_rows_sum(a.A.col, a.A.val, a.dx, tl, ipart, rs_all);
+    finish(tl[warp], E0);
+  } else if (nt > 0 && tl[0].e_log2 <= group_code(1)) {
     const int W = 1 << group_log2(tl[0].e_log2);
     const int q = warp / W, sub = warp % W;
     const bool has = q < nt;

@@ -66,6 +66,54 @@ __device__ __forceinline__ T stream_rounds(const int32_t* __restrict__ cp, const
   else return (acc[0] + acc[1]) + (acc[2] + acc[3]);
 }
 
+// A CTA whose kBlock / 32 tiles are all warp-streamed rows (kWarpLong) sums them together:
+// thread t takes row t % R (R = kBlock / 32 rows) and that row's nonzeros k = t / R + 32 i,
+// so one warp-wide load covers R neighbouring rows at 32 / R consecutive positions each. When
+// neighbouring rows have neighbouring columns at the same position (block-structured LPs:
+// transportation, assignment, multicommodity flows) a warp's gathers touch R x 32 / R
+// consecutive entries instead of 32 scattered ones. Row r's sum lands in rs_all[r][0]; the
+// order is fixed (positions per thread, then the thread's four-lane group, then warps).
+template <class T>
+__device__ __forceinline__ void interleaved_rows_sum(const int32_t* __restrict__ col, const T* __restrict__ val,
+                                                     const T* __restrict__ xg, const Tile* tl, T (*part)[kBlock / 32],
+                                                     T (*rs_all)[32]) {
+  constexpr int R = kBlock / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int r = threadIdx.x % R, u = threadIdx.x / R;
+  const int len = tl[r].nnz;
+  const int32_t* cp = col + tl[r].nnz_begin;
+  const T* vp = val + tl[r].nnz_begin;
+  int maxlen = 0;
+#pragma unroll
+  for (int q = 0; q < R; ++q) maxlen = max(maxlen, tl[q].nnz);
+  T acc = T(0);
+  for (int k0 = u; k0 < maxlen; k0 += 32 * kLongRound) {
+    int c[kLongRound];
+    T v[kLongRound];
+#pragma unroll
+    for (int j = 0; j < kLongRound; ++j) {
+      const int k = k0 + j * 32;
+      c[j] = k < len ? lds(cp + k) : 0;
+      v[j] = k < len ? lds(vp + k) : T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < kLongRound; ++j)
+      if (k0 + j * 32 < len) acc = fma(v[j], xg[c[j]], acc);
+  }
+  // lanes l, l + R, l + 2R, l + 3R of a warp hold row l
+#pragma unroll
+  for (int o = 16; o >= R; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane < R) part[warp][lane] = acc;
+  __syncthreads();
+  if (threadIdx.x < R) {
+    T sum = part[0][threadIdx.x];
+#pragma unroll
+    for (int w = 1; w < kBlock / 32; ++w) sum += part[w][threadIdx.x];
+    rs_all[threadIdx.x][0] = sum;
+  }
+  __syncthreads();
+}
+
 // One row of up to kWarpShare nonzeros summed by the whole warp (valid in lane 0).
 template <class T>
 __device__ __forceinline__ T long_row_sum(const int32_t* __restrict__ col, const T* __restrict__ val,

@@ -142,3 +142,22 @@ def test_ctypes_struct_sizes_match_header(tmp_path):
             C.sizeof(_abi.IterationStats), C.sizeof(_abi.Result), C.sizeof(_abi.LpDesc), C.sizeof(_abi.ServerConfig),
             _abi.Params.precision.offset, _abi.Result.last_iteration_stats.offset]
     assert got == want
+
+
+def test_reciprocal_division_is_correctly_rounded():
+    """The evaluation kernels divide by a vector or a weight sum through its reciprocal r = 1/b
+    and one correction step, q = a r, q' = q + (a - q b) r with both steps fused
+    multiply-adds (div_rcp in eval_kernels.cuh). The same arithmetic with libm's fma gives
+    IEEE a / b on random operands over a wide exponent range."""
+    libm = C.CDLL("libm.so.6")
+    fma = libm.fma
+    fma.restype = C.c_double
+    fma.argtypes = [C.c_double, C.c_double, C.c_double]
+    rng = np.random.default_rng(7)
+    a = rng.standard_normal(20000) * np.exp2(rng.integers(-60, 60, 20000))
+    b = np.abs(rng.standard_normal(20000)) * np.exp2(rng.integers(-60, 60, 20000)) + 1e-300
+    for ai, bi in zip(a.tolist(), b.tolist()):
+        r = 1.0 / bi
+        q = ai * r
+        q1 = fma(fma(-q, bi, ai), r, q)
+        assert q1 == ai / bi, (ai, bi)
