@@ -20,7 +20,7 @@ namespace gpdhg {
 template <int Q, unsigned MAXMASK, class F>
 __global__ void __launch_bounds__(kBlock) seg_reduce_kernel(const SegItem* items, const uint8_t* active, F f,
                                                             double* partials, int num_items) {
-  __shared__ double sh[Q * kBlock];
+  __shared__ double sh[(Q < kRedChunk ? Q : kRedChunk) * kBlock];
   __shared__ double res[Q];
   const SegItem it = items[blockIdx.x];
   if (!active[it.inst]) return;
@@ -36,7 +36,7 @@ template <int Q, unsigned MAXMASK>
 __global__ void __launch_bounds__(kBlock) seg_finalize_kernel(const int32_t* inst_item_begin, const uint8_t* active,
                                                               const double* partials, int num_items, double* out,
                                                               int out_stride) {
-  __shared__ double sh[Q * kBlock];
+  __shared__ double sh[(Q < kRedChunk ? Q : kRedChunk) * kBlock];
   __shared__ double res[Q];
   const int inst = blockIdx.x;
   if (!active[inst]) return;

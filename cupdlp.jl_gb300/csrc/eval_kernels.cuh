@@ -59,25 +59,32 @@ __device__ __forceinline__ double block_nan_max(double v, double* sh) {
 }
 
 // Q per-thread accumulators reduced over the CTA in a fixed order. The values go through
-// shared memory (sh: Q x kBlock doubles); warp w reduces quantities w, w + 8, ...: lane l
-// combines entry l of every warp in warp order, then a shuffle tree finishes (12 warp-wide
-// FP64 adds per summed quantity, where a shuffle tree in every warp takes 40; maxima run on
-// the integer pipe). Bit q of MAXMASK selects max (else sum). The result for q is valid in
-// thread q.
+// shared memory (sh: kRedChunk x kBlock doubles, kRedChunk quantities at a time); warp w
+// reduces quantities w, w + 8, ... of a chunk: lane l combines entry l of every warp in warp
+// order, then a shuffle tree finishes (12 warp-wide FP64 adds per summed quantity, where a
+// shuffle tree in every warp takes 40; maxima run on the integer pipe). Bit q of MAXMASK
+// selects max (else sum). A quantity's order does not depend on Q. The result for q is
+// valid in thread q (res: Q doubles).
+constexpr int kRedChunk = 16;
 template <int Q, unsigned MAXMASK>
 __device__ __forceinline__ double block_reduce_q(const double* acc, double* sh, double* res) {
+  static_assert(Q <= 32, "MAXMASK holds 32 quantities");
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
 #pragma unroll
-  for (int q = 0; q < Q; ++q) sh[q * kBlock + t] = acc[q];
-  __syncthreads();
-  for (int q = wid; q < Q; q += kBlock / 32) {
-    const bool is_max = (MAXMASK >> q) & 1u;
-    const double* c = sh + q * kBlock + lane;
-    double v = c[0];
+  for (int q0 = 0; q0 < Q; q0 += kRedChunk) {
+    if (q0 > 0) __syncthreads();  // the previous chunk's readers are done with sh
 #pragma unroll
-    for (int w = 1; w < kBlock / 32; ++w) v = is_max ? nan_max(v, c[w * 32]) : v + c[w * 32];
-    v = is_max ? warp_nan_max(v) : warp_sum(v);
-    if (lane == 0) res[q] = v;
+    for (int q = q0; q < Q && q < q0 + kRedChunk; ++q) sh[(q - q0) * kBlock + t] = acc[q];
+    __syncthreads();
+    for (int q = q0 + wid; q < Q && q < q0 + kRedChunk; q += kBlock / 32) {
+      const bool is_max = (MAXMASK >> q) & 1u;
+      const double* c = sh + (q - q0) * kBlock + lane;
+      double v = c[0];
+#pragma unroll
+      for (int w = 1; w < kBlock / 32; ++w) v = is_max ? nan_max(v, c[w * 32]) : v + c[w * 32];
+      v = is_max ? warp_nan_max(v) : warp_sum(v);
+      if (lane == 0) res[q] = v;
+    }
   }
   __syncthreads();
   return t < Q ? res[t] : 0.0;
@@ -129,9 +136,11 @@ struct EvalN {
   const double* ol;
   const double* ou;
   const double* oc;
-  __device__ __forceinline__ void operator()(long long j, double* a) const {
-    const double x = div_rcp((double)ax[j], var[j], rvar[j]);   // :470-471
-    const double g = (double)agrad[j] * var[j];    // :472-473
+  __device__ __forceinline__ void operator()(long long j, double* a) const { stats(j, ax[j], agrad[j], a); }
+  // the statistics of element j of the scaled point (axv, agv)
+  __device__ __forceinline__ void stats(long long j, T axv, T agv, double* a) const {
+    const double x = div_rcp((double)axv, var[j], rvar[j]);   // :470-471
+    const double g = (double)agv * var[j];         // :472-473
     const double l = ol[j], u = ou[j], c = oc[j];
     const bool fl = bits_finite(l), fu = bits_finite(u);
     const double lv = pos_part(l - x), uv = pos_part(x - u);
@@ -169,9 +178,10 @@ struct EvalM {
   const double* ob;
   int neq;
   const uint8_t* ineq_flag;  // per-row '>=' flag (packed batches); NULL: rows >= neq
-  __device__ __forceinline__ void operator()(long long i, double* a) const {
-    const double y = div_rcp((double)ay[i], con[i], rcon[i]);   // :474-475
-    const double kx = (double)akx[i] * con[i];     // :476-477
+  __device__ __forceinline__ void operator()(long long i, double* a) const { stats(i, ay[i], akx[i], a); }
+  __device__ __forceinline__ void stats(long long i, T ayv, T akv, double* a) const {
+    const double y = div_rcp((double)ayv, con[i], rcon[i]);   // :474-475
+    const double kx = (double)akv * con[i];        // :476-477
     const double b = ob[i];
     const bool ineq = ineq_flag ? ineq_flag[i] != 0 : i >= neq;
     double cv = b - kx;                            // :26-45
@@ -204,9 +214,24 @@ struct KktN {
   const T* c;
   const T* x0; const T* x1; const T* x2;
   const T* g0; const T* g1; const T* g2;
-  __device__ __forceinline__ void point(int p, const T* xs, const T* gs, long long j, double l, double u, double c,
-                                        bool fl, bool fu, double* a) const {
-    const double x = (double)xs[j], g = (double)gs[j];
+  __device__ __forceinline__ void operator()(long long j, double* a) const {
+    at(j, x0[j], g0[j], x1[j], g1[j], true, a);
+  }
+  // the three points' ingredients from the values of the current (xc, gc) and average
+  // (xa, ga) points; the last restart point's (quantities 8-11) only when with_restart
+  __device__ __forceinline__ void at(long long j, T xc, T gc, T xa, T ga, bool with_restart, double* a) const {
+    const double l = (double)this->l[j], u = (double)this->u[j], c = (double)this->c[j];
+    const bool fl = bits_finite(l), fu = bits_finite(u);
+    value_point(0, xc, gc, l, u, c, fl, fu, a);
+    value_point(1, xa, ga, l, u, c, fl, fu, a);
+    const T xr = x2[j];
+    if (with_restart) value_point(2, xr, g2[j], l, u, c, fl, fu, a);
+    const double d = (double)xa - (double)xr;
+    a[12] += d * d;
+  }
+  __device__ __forceinline__ void value_point(int p, T xv, T gv, double l, double u, double c, bool fl, bool fu,
+                                              double* a) const {
+    const double x = (double)xv, g = (double)gv;
     const double lv = pos_part(l - x), uv = pos_part(x - u);
     a[4 * p + 0] += lv * lv + uv * uv;
     a[4 * p + 1] += c * x;
@@ -214,15 +239,6 @@ struct KktN {
     const double rcv = g - rc;
     a[4 * p + 2] += rcv * rcv;
     a[4 * p + 3] += rc_contribution(rc, l, u);
-  }
-  __device__ __forceinline__ void operator()(long long j, double* a) const {
-    const double l = (double)this->l[j], u = (double)this->u[j], c = (double)this->c[j];
-    const bool fl = bits_finite(l), fu = bits_finite(u);
-    point(0, x0, g0, j, l, u, c, fl, fu, a);
-    point(1, x1, g1, j, l, u, c, fl, fu, a);
-    point(2, x2, g2, j, l, u, c, fl, fu, a);
-    const double d = (double)x1[j] - (double)x2[j];
-    a[12] += d * d;
   }
 };
 
@@ -233,9 +249,8 @@ struct KktM {
   const T* k0; const T* k1; const T* k2;
   int neq;
   const uint8_t* ineq_flag;  // as in EvalM
-  __device__ __forceinline__ void point(int p, const T* ys, const T* ks, long long i, double b, bool ineq,
-                                        double* a) const {
-    const double y = (double)ys[i], kx = (double)ks[i];
+  __device__ __forceinline__ void value_point(int p, T yv, T kv, double b, bool ineq, double* a) const {
+    const double y = (double)yv, kx = (double)kv;
     double cv = b - kx;
     if (ineq) cv = pos_part(cv);
     a[3 * p + 0] += cv * cv;
@@ -245,14 +260,87 @@ struct KktM {
     }
     a[3 * p + 2] += b * y;
   }
-  __device__ __forceinline__ void operator()(long long i, double* a) const {
+  __device__ __forceinline__ void operator()(long long i, double* a) const { at(i, y0[i], k0[i], y1[i], k1[i], true, a); }
+  __device__ __forceinline__ void at(long long i, T yc, T kc, T ya, T ka, bool with_restart, double* a) const {
     const double b = (double)this->b[i];
     const bool ineq = ineq_flag ? ineq_flag[i] != 0 : i >= neq;
-    point(0, y0, k0, i, b, ineq, a);
-    point(1, y1, k1, i, b, ineq, a);
-    point(2, y2, k2, i, b, ineq, a);
-    const double d = (double)y1[i] - (double)y2[i];
+    value_point(0, yc, kc, b, ineq, a);
+    value_point(1, ya, ka, b, ineq, a);
+    const T yr = y2[i];
+    if (with_restart) value_point(2, yr, k2[i], b, ineq, a);
+    const double d = (double)ya - (double)yr;
     a[9] += d * d;
+  }
+};
+
+// One evaluation's column pass (optimize(), src/primal_dual_hybrid_gradient_gpu.jl:633-760):
+// the average (compute_average!, src/saddle_point_gpu.jl:226-240; or the current point when
+// there is none, which takes the gradient buffer as it stood), its unscaled statistics
+// (EvalN), buffer_primal_gradient = c - K'y (:742), and the KKT ingredients of the current,
+// average and last-restart points (KktN). The last restart point's ingredients depend on
+// that point alone, so the caller recomputes them (with_restart) only after it changed.
+// Per element the arithmetic is that of the separate kernels, so the sums are the same.
+template <class T>
+struct EvalPassN {
+  EvalN<T> en;   // its ax / agrad are not read: the average comes from sx / skty here
+  KktN<T> kn;    // kn.x0 = x, kn.x2 = rx, kn.g2 = rgrad
+  const T* sx;
+  const T* skty;
+  const T* kty;
+  T* ax;         // the average, written
+  T* agrad;
+  T* grad;
+  double wx, wy, rwx, rwy;
+  int use_current;
+  int with_restart;
+  __device__ __forceinline__ void operator()(long long j, double* a) const {
+    const T c = kn.c[j];
+    const T gold = grad[j];
+    const T xc = kn.x0[j];
+    T xa, ga;
+    if (use_current) {
+      xa = xc;
+      ga = gold;
+    } else {
+      xa = (T)div_rcp((double)sx[j], wx, rwx);
+      const T g = (T)(-div_rcp((double)skty[j], wy, rwy));
+      ga = g + c;
+    }
+    ax[j] = xa;
+    agrad[j] = ga;
+    const T gc = c - kty[j];
+    grad[j] = gc;
+    en.stats(j, xa, ga, a);
+    kn.at(j, xc, gc, xa, ga, with_restart != 0, a + kEvalNQ);
+  }
+};
+
+// The row pass of the same evaluation: average (or current) y and K x, EvalM, KktM.
+template <class T>
+struct EvalPassM {
+  EvalM<T> em;   // its ay / akx are not read
+  KktM<T> km;    // km.y0 / km.k0 = current y / K x, km.y2 / km.k2 = restart point
+  const T* sy;
+  const T* skx;
+  T* ay;         // the average, written
+  T* akx;
+  double wx, wy, rwx, rwy;
+  int use_current;
+  int with_restart;
+  __device__ __forceinline__ void operator()(long long i, double* a) const {
+    const T yc = km.y0[i], kc = km.k0[i];
+    T ya, ka;
+    if (use_current) {
+      ya = yc;
+      ka = kc;
+    } else {
+      ya = (T)div_rcp((double)sy[i], wy, rwy);
+      ka = (T)div_rcp((double)skx[i], wx, rwx);
+    }
+    ay[i] = ya;
+    akx[i] = ka;
+    em.stats(i, ya, ka, a);
+    km.at(i, yc, kc, ya, ka, with_restart != 0, a + kEvalMQ);
   }
 };
 
@@ -261,25 +349,6 @@ struct KktM {
 template <class T>
 __global__ void grad_kernel(int n, const T* c, const T* kty, T* grad) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) grad[j] = c[j] - kty[j];
-}
-
-// compute_average!, src/saddle_point_gpu.jl:226-240 (rwx, rwy: the weight sums' reciprocals)
-template <class T>
-__global__ void average_n_kernel(int n, const T* sx, const T* skty, const T* c, double wx, double wy, double rwx,
-                                 double rwy, T* ax, T* agrad) {
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-    ax[j] = (T)div_rcp((double)sx[j], wx, rwx);
-    const T g = (T)(-div_rcp((double)skty[j], wy, rwy));
-    agrad[j] = g + c[j];
-  }
-}
-template <class T>
-__global__ void average_m_kernel(int m, const T* sy, const T* skx, double wx, double wy, double rwx, double rwy, T* ay,
-                                 T* akx) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-    ay[i] = (T)div_rcp((double)sy[i], wy, rwy);
-    akx[i] = (T)div_rcp((double)skx[i], wx, rwx);
-  }
 }
 
 // restart to average, src/saddle_point_gpu.jl:579-583

@@ -102,6 +102,10 @@ struct Workspace {
   DBuf<double> part_p, part_d, red_part, red_out;
   DBuf<double> rvar, rcon;   // 1 / variable and 1 / constraint rescaling (evaluation divisions)
   PinnedBuf<double> red_host;
+  // KKT ingredients of the last restart point (KktN quantities 8-11, KktM 6-8), valid until
+  // the restart point moves
+  bool restart_kkt_valid = false;
+  double restart_kkt_n[4] = {}, restart_kkt_m[3] = {};
   // segmented reductions over [0, n) and [0, m): the same layout a batch uses per instance
   DBuf<SegItem> seg_n, seg_m;
   DBuf<int32_t> seg_n_begin, seg_m_begin;
@@ -164,7 +168,7 @@ struct Workspace {
       };
       upload(seg_n, seg_n_begin, n, nseg_n);
       upload(seg_m, seg_m_begin, m, nseg_m);
-      red_part.alloc((size_t)16 * std::max(nseg_n, nseg_m));
+      red_part.alloc((size_t)32 * std::max(nseg_n, nseg_m));
       one.alloc(1);
       CK(cudaMemsetAsync(one.get(), 1, 1, s));
     }
@@ -354,36 +358,49 @@ bool run_phase(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopS
         st.pending_commit = 0;
       }
       const int p = st.parity;
-      // average (or the current point), src/primal_dual_hybrid_gradient_gpu.jl:635-642
-      if (st.numerical_error || st.count_primal == 0 || st.count_dual == 0) {
-        CK(cudaMemcpyAsync(W.ax.get(), W.x.get(), sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
-        CK(cudaMemcpyAsync(W.agrad.get(), W.grad.get(), sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
-        if (m) {
-          CK(cudaMemcpyAsync(W.ay.get(), W.ycur(p), sizeof(T) * m, cudaMemcpyDeviceToDevice, s));
-          CK(cudaMemcpyAsync(W.akx.get(), W.kxcur(p), sizeof(T) * m, cudaMemcpyDeviceToDevice, s));
-        }
+      // One pass per side (EvalPassN / EvalPassM): the average, or the current point
+      // (src/primal_dual_hybrid_gradient_gpu.jl:635-642); its unscaled statistics
+      // (src/iteration_stats_utils_gpu.jl:447-502); buffer_primal_gradient = c - K'y (:742);
+      // and the restart scheme's KKT ingredients, those of the last restart point only when
+      // it moved since they were computed. One read-back for all of them.
+      const bool use_current = st.numerical_error || st.count_primal == 0 || st.count_dual == 0;
+      const double wx = st.sum_w_primal, wy = st.sum_w_dual;
+      const double rwx = use_current ? 0.0 : 1.0 / wx, rwy = use_current ? 0.0 : 1.0 / wy;
+      const bool with_restart = !W.restart_kkt_valid;
+      W.template reduce<kEvalNQ + kKktNQ, kEvalNMax>(
+          true,
+          EvalPassN<T>{EvalN<T>{W.ax.get(), W.agrad.get(), P->var.get(), W.rvar.get(), P->ol.get(), P->ou.get(),
+                                P->oc.get()},
+                       KktN<T>{W.l, W.u, W.c, W.x.get(), W.ax.get(), W.rx.get(), W.grad.get(), W.agrad.get(),
+                               W.rgrad.get()},
+                       W.sx.get(), W.skty.get(), W.kty.get(), W.ax.get(), W.agrad.get(), W.grad.get(), wx, wy, rwx,
+                       rwy, use_current ? 1 : 0, with_restart ? 1 : 0},
+          0);
+      W.template reduce<kEvalMQ + kKktMQ, kEvalMMax>(
+          false,
+          EvalPassM<T>{EvalM<T>{W.ay.get(), W.akx.get(), P->con.get(), W.rcon.get(), P->ob.get(), P->neq, nullptr},
+                       KktM<T>{W.b, W.ycur(p), W.ay.get(), W.ry.get(), W.kxcur(p), W.akx.get(), W.rkx.get(), P->neq,
+                               nullptr},
+                       W.sy.get(), W.skx.get(), W.ay.get(), W.akx.get(), wx, wy, rwx, rwy, use_current ? 1 : 0,
+                       with_restart ? 1 : 0},
+          32);
+      W.fetch_reductions(32 + kEvalMQ + kKktMQ);
+      const double* en = W.red_host.p;            // EvalN, then KktN at kEvalNQ
+      const double* em = W.red_host.p + 32;       // EvalM, then KktM at kEvalMQ
+      double kn[kKktNQ], km[kKktMQ];
+      std::memcpy(kn, en + kEvalNQ, sizeof(kn));
+      std::memcpy(km, em + kEvalMQ, sizeof(km));
+      if (with_restart) {
+        std::memcpy(W.restart_kkt_n, kn + 8, sizeof(W.restart_kkt_n));
+        std::memcpy(W.restart_kkt_m, km + 6, sizeof(W.restart_kkt_m));
+        W.restart_kkt_valid = true;
       } else {
-        const double rwx = 1.0 / st.sum_w_primal, rwy = 1.0 / st.sum_w_dual;
-        average_n_kernel<T><<<gn, kBlock, 0, s>>>(n, W.sx.get(), W.skty.get(), W.c, st.sum_w_primal, st.sum_w_dual,
-                                                  rwx, rwy, W.ax.get(), W.agrad.get());
-        CK_LAUNCH();
-        ++P->launches;
-        if (m) {
-          average_m_kernel<T><<<gm, kBlock, 0, s>>>(m, W.sy.get(), W.skx.get(), st.sum_w_primal, st.sum_w_dual,
-                                                    rwx, rwy, W.ay.get(), W.akx.get());
-          CK_LAUNCH();
-          ++P->launches;
-        }
+        std::memcpy(kn + 8, W.restart_kkt_n, sizeof(W.restart_kkt_n));
+        std::memcpy(km + 6, W.restart_kkt_m, sizeof(W.restart_kkt_m));
       }
-      // unscaled statistics of the average, src/iteration_stats_utils_gpu.jl:447-502
-      W.template reduce<kEvalNQ, kEvalNMax>(true, EvalN<T>{W.ax.get(), W.agrad.get(), P->var.get(), W.rvar.get(),
-                                                         P->ol.get(), P->ou.get(), P->oc.get()}, 0);
-      W.template reduce<kEvalMQ, kEvalMMax>(false, EvalM<T>{W.ay.get(), W.akx.get(), P->con.get(), W.rcon.get(),
-                                                         P->ob.get(), P->neq, nullptr}, 16);
-      W.fetch_reductions(16 + kEvalMQ);
       gpdhg_iteration_stats stats;
       std::memset(&stats, 0, sizeof(stats));
-      assemble_stats(qi, prm, W.red_host.p, W.red_host.p + 16, stats);
+      assemble_stats(qi, prm, en, em, stats);
       stats.iteration_number = (int32_t)(it - 1);
       stats.cumulative_kkt_matrix_passes = st.kkt_passes;
       stats.cumulative_time_sec = L.elapsed();
@@ -454,20 +471,10 @@ bool run_phase(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopS
           return false;
         }
       }
-      // buffer_primal_gradient = c - K'y (:742)
-      grad_kernel<T><<<gn, kBlock, 0, s>>>(n, W.c, W.kty.get(), W.grad.get());
-      CK_LAUNCH();
-      ++P->launches;
-      // run_restart_scheme, src/saddle_point_gpu.jl:479-622
+      // run_restart_scheme, src/saddle_point_gpu.jl:479-622 (buffer_primal_gradient was
+      // refreshed by the column pass)
       int restart_used = GPDHG_RESTART_CHOICE_NO_RESTART;
       if (st.count_primal > 0 && st.count_dual > 0) {
-        W.template reduce<kKktNQ, 0u>(true, KktN<T>{W.l, W.u, W.c, W.x.get(), W.ax.get(), W.rx.get(), W.grad.get(),
-                                                 W.agrad.get(), W.rgrad.get()}, 0);
-        W.template reduce<kKktMQ, 0u>(false, KktM<T>{W.b, W.ycur(p), W.ay.get(), W.ry.get(), W.kxcur(p), W.akx.get(),
-                                                 W.rkx.get(), P->neq, nullptr}, 16);
-        W.fetch_reductions(16 + kKktMQ);
-        const double* kn = W.red_host.p;
-        const double* km = W.red_host.p + 16;
         const RestartDecision dec =
             decide_restart(prm, qi, st.count_primal, st.tau, st.omega, it - 1, kn, km, L.restart);
         if (dec.restart_used != GPDHG_RESTART_CHOICE_NO_RESTART) {
@@ -481,6 +488,7 @@ bool run_phase(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopS
               CK(cudaMemcpyAsync(W.kxcur_mut(p), W.akx.get(), sizeof(T) * m, cudaMemcpyDeviceToDevice, s));
             }
           }
+          W.restart_kkt_valid = false;  // the restart point moves below
           // reset_solution_weighted_average!
           CK(cudaMemsetAsync(W.sx.get(), 0, sizeof(T) * n, s));
           CK(cudaMemsetAsync(W.skty.get(), 0, sizeof(T) * n, s));
@@ -633,6 +641,7 @@ void init_state(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, Loop
   }
   st.iter_start_tau = st.tau;
   // create_last_restart_info
+  W.restart_kkt_valid = false;
   CK(cudaMemcpyAsync(W.rx.get(), W.x.get(), sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
   CK(cudaMemcpyAsync(W.rgrad.get(), W.grad.get(), sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
   if (m) {
@@ -676,6 +685,7 @@ void handoff_to_fp64(gpdhg_problem* P, Workspace<float>& F, Workspace<double>& D
   grad_kernel<double><<<D.grid_for(n), kBlock, 0, s>>>(n, D.c, D.kty.get(), D.grad.get());
   CK_LAUNCH();
   ++P->launches;
+  D.restart_kkt_valid = false;
   CK(cudaMemcpyAsync(D.rx.get(), D.x.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   CK(cudaMemcpyAsync(D.rgrad.get(), D.grad.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   if (m) {
