@@ -6,12 +6,15 @@ seeded synthetic data. One step = one full solve from the zero start to terminat
 under the reference's own criteria, with the scaled problem already resident in HBM.
 
   value       KKT matrix passes / s (the reference's cumulative_kkt_matrix_passes per
-              second of solve time), timed with CUDA events on the solver's stream.
+              second of solve time), timed with CUDA events on the solver's stream; the
+              solves run as they do for a user (evaluation intervals as CUDA graphs).
   e2e         the same metric through the C ABI with host buffers: gpdhg_problem_create
               (host->device copy of the CSR matrix and vectors, transpose and schedule),
               gpdhg_solve, and the device->host copy of the solution, every step.
   roofline    the dominant step kernel's algorithmic bytes / its CUDA-event time, measured
-              live over the timed steps (params.profile_kernels).
+              live right after the timed steps on the same number of solves launched kernel
+              by kernel with an event between every two (params.profile_kernels; events
+              cannot split the kernels of a CUDA graph).
   cpu_baseline  the oracle (the CPU FP64 restatement of the reference loop) on the host
               cores over a bounded sample of the same workload.
 
@@ -483,16 +486,15 @@ def run_ours(args):
     for _ in range(args.warmup):
         dp.solve(params, want_solution=False)
 
-    params.profile_kernels = True
     cparams = cupdlp.params_to_c(params)
-    cparams.profile_kernels = 1
     import ctypes as C
     from cupdlp import _abi
-    results = []
-    ms_total = 0.0
-    barrier(pg)
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
+
+    def timed_solves(profile):
+        # solves with the inputs resident, each bracketed by CUDA events on the problem's
+        # stream, L2 flushed before each
+        cparams.profile_kernels = 1 if profile else 0
+        out, ms = [], 0.0
         for _ in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
@@ -503,8 +505,14 @@ def run_ours(args):
             _abi.check(dp.lib.gpdhg_solve(dp.handle, C.byref(cparams), C.byref(res), None, None), dp.lib)
             e1.record(stream)
             e1.synchronize()
-            ms_total += e0.elapsed_time(e1)
-            results.append(res)
+            ms += e0.elapsed_time(e1)
+            out.append(res)
+        return out, ms
+
+    barrier(pg)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        results, ms_total = timed_solves(profile=False)
     torch.cuda.synchronize()
     barrier(pg)
     clocks = clk.summary()
@@ -514,12 +522,15 @@ def run_ours(args):
     value = kkt_all / t_max
     launches = sum(r.kernels_launched for r in results)
 
-    # roofline of the dominant step kernel, from the live per-kernel CUDA events
+    # roofline of the dominant step kernel: the same solves again with a CUDA event between
+    # every two step kernels (launched one by one: events inside a CUDA graph cannot split
+    # its kernels), per-kernel durations summed over all attempts
+    prof, _ = timed_solves(profile=True)
     bm = bytes_model(m, n, nnz, 0 if prec == cupdlp.Precision.FP64 else 1)
-    attempts = sum(r.primal_kernel_launches for r in results)
-    spmv = sum(r.primal_spmv_launches for r in results)
-    tp = sum(r.primal_kernel_sec for r in results)
-    td = sum(r.dual_kernel_sec for r in results)
+    attempts = sum(r.primal_kernel_launches for r in prof)
+    spmv = sum(r.primal_spmv_launches for r in prof)
+    tp = sum(r.primal_kernel_sec for r in prof)
+    td = sum(r.dual_kernel_sec for r in prof)
     bytes_p = spmv * bm["primal_commit"] + (attempts - spmv) * bm["primal_plain"]
     bytes_d = attempts * bm["dual"] + spmv * bm["dual_commit_extra"]
     peaks = {}

@@ -1,0 +1,199 @@
+// ingest.cu — A' of an uploaded CSR matrix, built on the GPU.
+//
+// The reference builds the transpose with CuSparseMatrixCSR(A') (src/cpu_to_gpu.jl:46).
+// Here a stable LSD radix sort of the nonzeros by column (8-bit digits) yields, for every
+// column, its nonzeros in increasing row order, which is exactly the host counting sort's
+// order (transpose_csr): A' is the same matrix entry for entry and in the same storage order,
+// so every SpMV over it sums in the same order as before.
+//
+// One pass = a digit histogram per 4,096-key tile, one exclusive scan over (digit, tile), and
+// a scatter in which every tile places its keys in order: per round of 256 keys each warp
+// ranks its lanes among equal digits (__match_any_sync), a per-digit prefix over the warps
+// orders the warps, and a per-digit running base orders the rounds. Stable by construction
+// and deterministic (no atomics decide a position).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "problem.h"
+
+namespace gpdhg {
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;
+constexpr int kDigits = 256;
+
+// rows[k] = the row of nonzero k (the last row i with rp[i] <= k; empty rows share offsets)
+__global__ void row_of_kernel(int32_t m, long long nnz, const int32_t* __restrict__ rp, int32_t* __restrict__ rows) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = m - 1;  // rp[lo] <= k < rp[m]
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (rp[mid] <= k) lo = mid;
+      else hi = mid - 1;
+    }
+    rows[k] = lo;
+  }
+}
+
+__global__ void iota_kernel(long long len, uint32_t* __restrict__ v) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < len; k += (long long)gridDim.x * blockDim.x)
+    v[k] = (uint32_t)k;
+}
+
+// hist[d * tiles + t] = keys of tile t whose digit is d
+__global__ void __launch_bounds__(kSortThreads) digit_hist_kernel(const uint32_t* __restrict__ keys, long long len,
+                                                                  int shift, uint32_t* __restrict__ hist, int tiles) {
+  __shared__ uint32_t h[kDigits];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * kSortTile;
+  for (int i = threadIdx.x; i < kSortTile; i += kSortThreads) {
+    const long long k = base + i;
+    if (k < len) atomicAdd(&h[(keys[k] >> shift) & (kDigits - 1)], 1u);
+  }
+  __syncthreads();
+  hist[(size_t)threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// In-place exclusive scan of len counts (one CTA: contiguous chunks per thread, then a scan
+// of the chunk totals).
+__global__ void __launch_bounds__(1024) exclusive_scan_kernel(uint32_t* __restrict__ v, long long len) {
+  __shared__ uint32_t part[1024];
+  const long long chunk = (len + 1023) / 1024;
+  const long long b = threadIdx.x * chunk, e = min(len, b + chunk);
+  uint32_t s = 0;
+  for (long long i = b; i < e; ++i) s += v[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int t = 0; t < 1024; ++t) {
+      const uint32_t c = part[t];
+      part[t] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  uint32_t run = part[threadIdx.x];
+  for (long long i = b; i < e; ++i) {
+    const uint32_t c = v[i];
+    v[i] = run;
+    run += c;
+  }
+}
+
+__global__ void __launch_bounds__(kSortThreads) digit_scatter_kernel(const uint32_t* __restrict__ keys,
+                                                                     const uint32_t* __restrict__ vals, long long len,
+                                                                     int shift, const uint32_t* __restrict__ offs,
+                                                                     int tiles, uint32_t* __restrict__ keys_out,
+                                                                     uint32_t* __restrict__ vals_out) {
+  __shared__ uint32_t base[kDigits];                        // next output position per digit
+  __shared__ uint32_t wcnt[kSortThreads / 32][kDigits];     // a round's per-warp digit counts
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  base[t] = offs[(size_t)t * tiles + blockIdx.x];
+  const long long tile0 = (long long)blockIdx.x * kSortTile;
+  for (int r = 0; r < kSortItems; ++r) {
+    const long long k = tile0 + (long long)r * kSortThreads + t;
+    const bool in = k < len;
+    const uint32_t key = in ? keys[k] : 0u, val = in ? vals[k] : 0u;
+    const int d = in ? (int)((key >> shift) & (kDigits - 1)) : kDigits;  // out-of-range lanes: a digit of their own
+#pragma unroll
+    for (int w = 0; w < kSortThreads / 32; ++w) wcnt[w][t] = 0;
+    __syncthreads();
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    if (in && rank == 0) wcnt[warp][d] = __popc(peers);
+    __syncthreads();
+    uint32_t run = 0;  // thread t: exclusive prefix of digit t over the warps
+#pragma unroll
+    for (int w = 0; w < kSortThreads / 32; ++w) {
+      const uint32_t c = wcnt[w][t];
+      wcnt[w][t] = run;
+      run += c;
+    }
+    __syncthreads();
+    if (in) {
+      const uint32_t dst = base[d] + wcnt[warp][d] + (uint32_t)rank;
+      keys_out[dst] = key;
+      vals_out[dst] = val;
+    }
+    __syncthreads();
+    base[t] += run;
+  }
+}
+
+// A' = (row_ptr from the sorted columns, col = row of the nonzero, val)
+__global__ void transpose_fill_kernel(long long nnz, const uint32_t* __restrict__ perm, const int32_t* __restrict__ rows,
+                                      const double* __restrict__ val, int32_t* __restrict__ col_t,
+                                      double* __restrict__ val_t) {
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < nnz; p += (long long)gridDim.x * blockDim.x) {
+    const uint32_t k = perm[p];
+    col_t[p] = rows[k];
+    val_t[p] = val[k];
+  }
+}
+
+__global__ void transpose_rowptr_kernel(long long nnz, int32_t n, const uint32_t* __restrict__ skeys,
+                                        int32_t* __restrict__ rp_t) {
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p <= nnz; p += (long long)gridDim.x * blockDim.x) {
+    const long long prev = p == 0 ? -1 : (long long)skeys[p - 1];
+    const long long cur = p == nnz ? (long long)n : (long long)skeys[p];
+    for (long long j = prev + 1; j <= cur; ++j) rp_t[j] = (int32_t)p;
+  }
+}
+
+int grid_of(long long len) { return (int)std::max<long long>(1, std::min<long long>((len + 255) / 256, 8192)); }
+
+}  // namespace
+
+void transpose_on_device(const DeviceMatrix& A, DeviceMatrix& At, cudaStream_t s) {
+  const int32_t m = A.nrows, n = A.ncols;
+  const long long nnz = A.nnz;
+  At.nrows = n;
+  At.ncols = m;
+  At.nnz = nnz;
+  At.row_ptr.alloc((size_t)n + 1);
+  At.col.alloc(std::max<long long>(nnz, 1));
+  At.val64.alloc(std::max<long long>(nnz, 1));
+  DBuf<uint32_t> k0(std::max<long long>(nnz, 1)), k1(std::max<long long>(nnz, 1));
+  DBuf<uint32_t> v0(std::max<long long>(nnz, 1)), v1(std::max<long long>(nnz, 1));
+  DBuf<int32_t> rows(std::max<long long>(nnz, 1));
+  DBuf<uint32_t> hist;
+  if (nnz > 0) {
+    row_of_kernel<<<grid_of(nnz), 256, 0, s>>>(m, nnz, A.row_ptr.get(), rows.get());
+    CK_LAUNCH();
+    CK(cudaMemcpyAsync(k0.get(), A.col.get(), sizeof(uint32_t) * nnz, cudaMemcpyDeviceToDevice, s));
+    iota_kernel<<<grid_of(nnz), 256, 0, s>>>(nnz, v0.get());
+    CK_LAUNCH();
+    const int tiles = (int)((nnz + kSortTile - 1) / kSortTile);
+    hist.alloc((size_t)kDigits * tiles);
+    uint32_t *ka = k0.get(), *kb = k1.get(), *va = v0.get(), *vb = v1.get();
+    for (int shift = 0; shift < 32 && n > 1 && ((uint32_t)(n - 1) >> shift) != 0u; shift += 8) {
+      digit_hist_kernel<<<tiles, kSortThreads, 0, s>>>(ka, nnz, shift, hist.get(), tiles);
+      CK_LAUNCH();
+      exclusive_scan_kernel<<<1, 1024, 0, s>>>(hist.get(), (long long)kDigits * tiles);
+      CK_LAUNCH();
+      digit_scatter_kernel<<<tiles, kSortThreads, 0, s>>>(ka, va, nnz, shift, hist.get(), tiles, kb, vb);
+      CK_LAUNCH();
+      std::swap(ka, kb);
+      std::swap(va, vb);
+    }
+    transpose_fill_kernel<<<grid_of(nnz), 256, 0, s>>>(nnz, va, rows.get(), A.val64.get(), At.col.get(),
+                                                       At.val64.get());
+    CK_LAUNCH();
+    transpose_rowptr_kernel<<<grid_of(nnz + 1), 256, 0, s>>>(nnz, n, ka, At.row_ptr.get());
+    CK_LAUNCH();
+  } else {
+    CK(cudaMemsetAsync(At.row_ptr.get(), 0, sizeof(int32_t) * ((size_t)n + 1), s));
+  }
+  At.host_rp.resize((size_t)n + 1);
+  CK(cudaMemcpyAsync(At.host_rp.data(), At.row_ptr.get(), sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
+  // the sort buffers are freed at return: wait for the kernels that use them (and the copy)
+  CK(cudaStreamSynchronize(s));
+}
+
+}  // namespace gpdhg

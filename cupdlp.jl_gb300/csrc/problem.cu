@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 #include "problem.h"
 
@@ -58,8 +59,8 @@ void transpose_csr(int32_t m, int32_t n, const int32_t* rp, const int32_t* col, 
 
 namespace {
 
-void upload_matrix(DeviceMatrix& dm, int32_t nrows, int32_t ncols, const int32_t* rp, const int32_t* col,
-                   const double* val, cudaStream_t s) {
+void upload_csr(DeviceMatrix& dm, int32_t nrows, int32_t ncols, const int32_t* rp, const int32_t* col,
+                const double* val, cudaStream_t s) {
   dm.nrows = nrows;
   dm.ncols = ncols;
   dm.nnz = rp[nrows];
@@ -72,7 +73,11 @@ void upload_matrix(DeviceMatrix& dm, int32_t nrows, int32_t ncols, const int32_t
     CK(cudaMemcpyAsync(dm.col.get(), col, sizeof(int32_t) * dm.nnz, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(dm.val64.get(), val, sizeof(double) * dm.nnz, cudaMemcpyHostToDevice, s));
   }
-  std::vector<RowItem> items = build_row_items(rp, nrows);
+}
+
+// The row-block schedule of the plain SpMV, from the matrix's host row pointer.
+void set_row_items(DeviceMatrix& dm, cudaStream_t s) {
+  std::vector<RowItem> items = build_row_items(dm.host_rp.data(), dm.nrows);
   if (items.empty()) items.push_back({0, 0, 1, kItemStaged, 0, 0});  // no rows: one idle CTA still runs the step decision
   dm.num_items = (int32_t)items.size();
   dm.items.alloc(std::max<size_t>(items.size(), 1));
@@ -104,6 +109,39 @@ double norm_inf(const double* v, size_t n) {
 
 }  // namespace
 
+namespace {
+
+// The smallest k in [0, len) with bad(k), or -1: contiguous chunks checked on host threads,
+// so the answer (and hence the error reported) is the serial scan's.
+template <class Bad>
+int64_t first_bad(int64_t len, Bad bad) {
+  const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
+  const int T = (int)std::min<int64_t>(std::min<int64_t>(hw, 32), std::max<int64_t>(1, len / 65536));
+  if (T <= 1) {
+    for (int64_t k = 0; k < len; ++k)
+      if (bad(k)) return k;
+    return -1;
+  }
+  std::vector<int64_t> first(T, -1);
+  std::vector<std::thread> th;
+  th.reserve(T);
+  for (int t = 0; t < T; ++t)
+    th.emplace_back([&, t] {
+      const int64_t b = len * t / T, e = len * (t + 1) / T;
+      for (int64_t k = b; k < e; ++k)
+        if (bad(k)) {
+          first[t] = k;
+          return;
+        }
+    });
+  for (auto& x : th) x.join();
+  for (int t = 0; t < T; ++t)
+    if (first[t] >= 0) return first[t];
+  return -1;
+}
+
+}  // namespace
+
 // validate (src/preprocess.jl:8-74) for the LP descriptor, plus structural CSR checks
 // the reference gets from SparseMatrixCSC's invariants.
 void validate_lp_desc(const gpdhg_lp_desc* d) {
@@ -117,25 +155,31 @@ void validate_lp_desc(const gpdhg_lp_desc* d) {
     throw Error(GPDHG_ERR_INVALID_ARGUMENT, "required array pointer is NULL");
   const int32_t m = d->num_constraints, n = d->num_variables;
   if (d->row_ptr[0] != 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "row_ptr[0] must be 0");
-  for (int32_t i = 0; i < m; ++i)
-    if (d->row_ptr[i + 1] < d->row_ptr[i]) throw Error(GPDHG_ERR_INVALID_PROBLEM, "row_ptr is not monotone");
+  if (first_bad(m, [&](int64_t i) { return d->row_ptr[i + 1] < d->row_ptr[i]; }) >= 0)
+    throw Error(GPDHG_ERR_INVALID_PROBLEM, "row_ptr is not monotone");
   const int64_t nnz = d->row_ptr[m];
   if (nnz != d->nnz) throw Error(GPDHG_ERR_INVALID_PROBLEM, "nnz does not match row_ptr[m]");
   if (nnz > 0 && (!d->col_idx || !d->values)) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "col_idx/values NULL");
-  for (int64_t k = 0; k < nnz; ++k) {
-    if (d->col_idx[k] < 0 || d->col_idx[k] >= n) throw Error(GPDHG_ERR_INVALID_PROBLEM, "column index out of range");
-    if (!std::isfinite(d->values[k])) throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN or Inf found in constraint matrix");
+  {
+    auto bad_col = [&](int64_t k) { return d->col_idx[k] < 0 || d->col_idx[k] >= n; };
+    const int64_t k = first_bad(nnz, [&](int64_t q) { return bad_col(q) || !std::isfinite(d->values[q]); });
+    if (k >= 0) {
+      if (bad_col(k)) throw Error(GPDHG_ERR_INVALID_PROBLEM, "column index out of range");
+      throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN or Inf found in constraint matrix");
+    }
   }
   auto check_bounds = [&](const double* l, const double* u) {
-    for (int32_t j = 0; j < n; ++j) {
-      if (l[j] == INFINITY) throw Error(GPDHG_ERR_INVALID_PROBLEM, "variable_lower_bound contains +Inf");
-      if (u[j] == -INFINITY) throw Error(GPDHG_ERR_INVALID_PROBLEM, "variable_upper_bound contains -Inf");
-      if (std::isnan(l[j]) || std::isnan(u[j])) throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN found in variable bounds");
-    }
+    const int64_t j = first_bad(n, [&](int64_t q) {
+      return l[q] == INFINITY || u[q] == -INFINITY || std::isnan(l[q]) || std::isnan(u[q]);
+    });
+    if (j < 0) return;
+    if (l[j] == INFINITY) throw Error(GPDHG_ERR_INVALID_PROBLEM, "variable_lower_bound contains +Inf");
+    if (u[j] == -INFINITY) throw Error(GPDHG_ERR_INVALID_PROBLEM, "variable_upper_bound contains -Inf");
+    throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN found in variable bounds");
   };
   auto check_finite = [&](const double* v, int32_t len, const char* what) {
-    for (int32_t k = 0; k < len; ++k)
-      if (!std::isfinite(v[k])) throw Error(GPDHG_ERR_INVALID_PROBLEM, std::string("NaN or Inf found in ") + what);
+    if (first_bad(len, [&](int64_t q) { return !std::isfinite(v[q]); }) >= 0)
+      throw Error(GPDHG_ERR_INVALID_PROBLEM, std::string("NaN or Inf found in ") + what);
   };
   check_bounds(d->variable_lower_bound, d->variable_upper_bound);
   check_finite(d->objective_vector, n, "objective vector");
@@ -146,9 +190,8 @@ void validate_lp_desc(const gpdhg_lp_desc* d) {
   if (d->original_objective_vector) check_finite(d->original_objective_vector, n, "original objective vector");
   if (d->original_right_hand_side && m) check_finite(d->original_right_hand_side, m, "original right hand side");
   auto check_pos = [&](const double* v, int32_t len, const char* what) {
-    for (int32_t k = 0; k < len; ++k)
-      if (!(v[k] > 0.0) || !std::isfinite(v[k]))
-        throw Error(GPDHG_ERR_INVALID_PROBLEM, std::string(what) + " must be positive and finite");
+    if (first_bad(len, [&](int64_t q) { return !(v[q] > 0.0) || !std::isfinite(v[q]); }) >= 0)
+      throw Error(GPDHG_ERR_INVALID_PROBLEM, std::string(what) + " must be positive and finite");
   };
   if (d->constraint_rescaling && m) check_pos(d->constraint_rescaling, m, "constraint_rescaling");
   if (d->variable_rescaling) check_pos(d->variable_rescaling, n, "variable_rescaling");
@@ -165,34 +208,41 @@ void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d) {
   CK(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
   cudaStream_t s = p->stream;
 
-  upload_matrix(p->A, m, n, d->row_ptr, d->col_idx, d->values, s);
-  HostCsr t;
-  transpose_csr(m, n, d->row_ptr, d->col_idx, d->values, t);
-  upload_matrix(p->At, n, m, t.row_ptr.data(), t.col.data(), t.val.data(), s);
-
-  std::vector<double> ones((size_t)std::max(m, n), 1.0);
-  upload_vec(p->l, d->variable_lower_bound, n, s);
-  upload_vec(p->u, d->variable_upper_bound, n, s);
-  upload_vec(p->c, d->objective_vector, n, s);
-  upload_vec(p->b, d->right_hand_side, m, s);
-  upload_vec_or_fill(p->ol, d->original_variable_lower_bound, d->variable_lower_bound, n, s);
-  upload_vec_or_fill(p->ou, d->original_variable_upper_bound, d->variable_upper_bound, n, s);
-  upload_vec_or_fill(p->oc, d->original_objective_vector, d->objective_vector, n, s);
-  upload_vec_or_fill(p->ob, d->original_right_hand_side, d->right_hand_side, m, s);
-  upload_vec_or_fill(p->con, d->constraint_rescaling, ones.data(), m, s);
-  upload_vec_or_fill(p->var, d->variable_rescaling, ones.data(), n, s);
-
-  double amax = 0.0;
-  for (int64_t k = 0; k < d->nnz; ++k) amax = std::max(amax, std::fabs(d->values[k]));
-  p->amax = amax;
-  p->norm2_c_scaled = norm2(d->objective_vector, n);
-  p->norm2_b_scaled = m ? norm2(d->right_hand_side, m) : 0.0;
-  const double* oc = d->original_objective_vector ? d->original_objective_vector : d->objective_vector;
-  const double* ob = d->original_right_hand_side ? d->original_right_hand_side : d->right_hand_side;
-  p->linf_c = norm_inf(oc, n);
-  p->l2_c = norm2(oc, n);
-  p->linf_b = m ? norm_inf(ob, m) : 0.0;
-  p->l2_b = m ? norm2(ob, m) : 0.0;
+  // host scalars on a helper thread while the device builds A' (serial sums, as before)
+  std::thread scalars([p, d, m, n] {
+    double amax = 0.0;
+    for (int64_t k = 0; k < d->nnz; ++k) amax = std::max(amax, std::fabs(d->values[k]));
+    p->amax = amax;
+    p->norm2_c_scaled = norm2(d->objective_vector, n);
+    p->norm2_b_scaled = m ? norm2(d->right_hand_side, m) : 0.0;
+    const double* oc = d->original_objective_vector ? d->original_objective_vector : d->objective_vector;
+    const double* ob = d->original_right_hand_side ? d->original_right_hand_side : d->right_hand_side;
+    p->linf_c = norm_inf(oc, n);
+    p->l2_c = norm2(oc, n);
+    p->linf_b = m ? norm_inf(ob, m) : 0.0;
+    p->l2_b = m ? norm2(ob, m) : 0.0;
+  });
+  try {
+    upload_csr(p->A, m, n, d->row_ptr, d->col_idx, d->values, s);
+    transpose_on_device(p->A, p->At, s);
+    std::vector<double> ones((size_t)std::max(m, n), 1.0);
+    upload_vec(p->l, d->variable_lower_bound, n, s);
+    upload_vec(p->u, d->variable_upper_bound, n, s);
+    upload_vec(p->c, d->objective_vector, n, s);
+    upload_vec(p->b, d->right_hand_side, m, s);
+    upload_vec_or_fill(p->ol, d->original_variable_lower_bound, d->variable_lower_bound, n, s);
+    upload_vec_or_fill(p->ou, d->original_variable_upper_bound, d->variable_upper_bound, n, s);
+    upload_vec_or_fill(p->oc, d->original_objective_vector, d->objective_vector, n, s);
+    upload_vec_or_fill(p->ob, d->original_right_hand_side, d->right_hand_side, m, s);
+    upload_vec_or_fill(p->con, d->constraint_rescaling, ones.data(), m, s);
+    upload_vec_or_fill(p->var, d->variable_rescaling, ones.data(), n, s);
+    set_row_items(p->A, s);
+    set_row_items(p->At, s);
+  } catch (...) {
+    scalars.join();
+    throw;
+  }
+  scalars.join();
   CK(cudaStreamSynchronize(s));
 }
 

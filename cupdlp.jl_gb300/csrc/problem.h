@@ -69,6 +69,12 @@ std::vector<RowItem> build_row_items(const int32_t* row_ptr, int32_t nrows);
 // CSR of A' from CSR of A (counting sort, stable in row order).
 void transpose_csr(int32_t m, int32_t n, const int32_t* rp, const int32_t* col, const double* val, HostCsr& out);
 
+// The same A' built on the GPU from an uploaded A (ingest.cu: a stable radix sort by
+// column); fills At's device arrays and its host row pointer. Its row-block schedule is the
+// caller's (set_row_items).
+struct DeviceMatrix;
+void transpose_on_device(const DeviceMatrix& A, DeviceMatrix& At, cudaStream_t s);
+
 struct DeviceMatrix {
   int32_t nrows = 0, ncols = 0;
   long long nnz = 0;

@@ -16,6 +16,9 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <memory>
+#include <mutex>
+#include <thread>
 #include <limits>
 #include <random>
 #include <type_traits>
@@ -80,13 +83,36 @@ inline int graph_level(int remaining) {
 // Host table of the step-size factors (1 - (k+1)^-r, 1 + (k+1)^-g) of take_step!
 // (:405-407): the device reads it instead of evaluating two FP64 pow() per attempt in one
 // thread, and the values are the host libm's, as in the reference's host-side loop.
+// The table of an exponent pair is computed once per process (on host threads, each entry
+// by the same libm call whatever the thread) and kept for later problems.
 void fill_pow_table(std::vector<double>& t, double r, double g) {
-  t.resize(2 * kPowTableLen);
-  for (long long k = 0; k < kPowTableLen; ++k) {
-    const double k1 = (double)(k + 1);
-    t[2 * k] = 1.0 - 1.0 / std::pow(k1, r);
-    t[2 * k + 1] = 1.0 + 1.0 / std::pow(k1, g);
+  static std::mutex mu;
+  static std::vector<std::pair<std::pair<double, double>, std::shared_ptr<const std::vector<double>>>> cache;
+  std::shared_ptr<const std::vector<double>> hit;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    for (auto& e : cache)
+      if (e.first.first == r && e.first.second == g) hit = e.second;
   }
+  if (!hit) {
+    auto v = std::make_shared<std::vector<double>>(2 * kPowTableLen);
+    const int T = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (int q = 0; q < T; ++q)
+      th.emplace_back([&, q] {
+        for (long long k = kPowTableLen * q / T; k < kPowTableLen * (q + 1) / T; ++k) {
+          const double k1 = (double)(k + 1);
+          (*v)[2 * k] = 1.0 - 1.0 / std::pow(k1, r);
+          (*v)[2 * k + 1] = 1.0 + 1.0 / std::pow(k1, g);
+        }
+      });
+    for (auto& x : th) x.join();
+    std::lock_guard<std::mutex> lock(mu);
+    if (cache.size() >= 8) cache.erase(cache.begin());
+    cache.push_back({{r, g}, v});
+    hit = v;
+  }
+  t = *hit;
 }
 
 template <class T>
