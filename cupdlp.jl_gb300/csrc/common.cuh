@@ -97,6 +97,7 @@ struct StepState {
   long long pow_table_len;
   // written in every attempt by the instance's first dual CTA, for the deciding CTA:
   double half_w_dx2;       // 0.5 * omega * ||dx|| * ||dx||: the primal part of the movement
+  double half_over_omega;  // 0.5 / omega
   double f1, f2;           // step-size factors for this attempt's counter
   // 1 / sum_w_primal and 1 / sum_w_dual, set by the host before an evaluation averages
   double rcp_w_primal, rcp_w_dual;

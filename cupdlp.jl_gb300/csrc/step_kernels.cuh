@@ -272,10 +272,10 @@ __device__ __forceinline__ double half_w_dx2(double omega, double dx2) {
 
 // Decision of take_step! for one attempt, on a copy of the instance's state (the caller
 // writes it back). f1 / f2 are the step-size factors (1 - (k+1)^-r), (1 + (k+1)^-g)
-// for the attempt counter after this attempt and hw_dx2 = half_w_dx2(omega, ||dx||^2),
-// all prepared by the instance's first dual CTA while the others still run.
+// for the attempt counter after this attempt, hw_dx2 = half_w_dx2(omega, ||dx||^2) and
+// hoo = 0.5 / omega, all prepared by the instance's first dual CTA while the others still run.
 __device__ __forceinline__ void step_decision(StepState& s, double f1, double f2, double inter_signed, double hw_dx2,
-                                              double dy2) {
+                                              double hoo, double dy2) {
   s.total_iters += s.constant_step ? 0 : 1;
   s.kkt_passes += 1.0;
   s.attempts_in_chunk += 1;
@@ -283,7 +283,7 @@ __device__ __forceinline__ void step_decision(StepState& s, double f1, double f2
   const double tau = s.tau;
   const double inter = fabs(inter_signed);
   const double ndy = sqrt(dy2);
-  const double movement = hw_dx2 + (0.5 / omega) * ndy * ndy;
+  const double movement = hw_dx2 + hoo * ndy * ndy;
   double limit;
   bool accept;
   if (s.constant_step) {
@@ -493,6 +493,7 @@ __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualA
         double f1, f2;
         step_factors(*st, st->total_iters + (st->constant_step ? 0 : 1), f1, f2);
         stw->half_w_dx2 = half_w_dx2(st->omega, ox[0]);
+        stw->half_over_omega = 0.5 / st->omega;
         stw->f1 = f1;
         stw->f2 = f2;
       }
@@ -548,9 +549,12 @@ __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualA
     s.arrive = 0;
     if (pending) s.primal_spmv += 1;
     s.pending_commit = 0;
-    step_decision(s, s.f1, s.f2, tot[0], s.half_w_dx2, tot[1]);
-    *stw = s;
+    step_decision(s, s.f1, s.f2, tot[0], s.half_w_dx2, s.half_over_omega, tot[1]);
   }
+  __syncthreads();
+  // the new state back to global memory, one 8-byte word per thread
+  if (threadIdx.x < sizeof(StepState) / 8)
+    reinterpret_cast<unsigned long long*>(stw)[threadIdx.x] = reinterpret_cast<const unsigned long long*>(&s)[threadIdx.x];
 }
 
 // Launches a step kernel with programmatic dependent launch enabled (see pdl_wait).
