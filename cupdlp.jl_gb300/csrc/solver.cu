@@ -371,6 +371,12 @@ bool run_phase(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopS
     CK(cudaMemcpyAsync(W.st_dev.get(), W.st_host.p, sizeof(StepState), cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
   };
+  // The same copy when the mirror stays untouched until the stream has passed it (the step
+  // graphs that follow end by copying the state back into the mirror, and the host reads it
+  // only after synchronising with them).
+  auto push_state_async = [&]() {
+    CK(cudaMemcpyAsync(W.st_dev.get(), W.st_host.p, sizeof(StepState), cudaMemcpyHostToDevice, s));
+  };
 
   while (true) {
     const long long it = L.iteration;
@@ -547,7 +553,7 @@ bool run_phase(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopS
     st.max_attempts_in_chunk = 1 << 30;
     st.iter_start_tau = st.tau;
     st.arrive = 0;
-    push_state();
+    push_state_async();
     const auto tb = Clock::now();
     long long launches = 0;
     const bool prof = prm.profile_kernels != 0;

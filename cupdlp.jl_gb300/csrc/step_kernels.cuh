@@ -155,11 +155,13 @@ __global__ void __launch_bounds__(kBlock, kPrimalCtasPerSm<T>) primal_step_kerne
   __shared__ Tile tl[kTilesPerCtaMax];
   const int b = a.plan.cta_map ? a.plan.cta_map[blockIdx.x] : (int)blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // programmatic dependent launch: let the next kernel's CTAs launch once all of ours have
-  // started, stage the constant tile descriptors, and only then wait for the previous kernel
-  pdl_launch_dependents();
+  // programmatic dependent launch: stage the constant tile descriptors, wait for the previous
+  // kernel, and only then let the next (dual) kernel's CTAs launch: once all of ours have
+  // passed this point, the state the previous dual kernel wrote is complete, so the dual
+  // kernel may read it before its own wait (this kernel never writes it)
   const int nt = stage_tiles(a.plan.tiles, a.plan.cta_tile_begin[b], a.plan.cta_tile_begin[b + 1], tl);
   pdl_wait();
+  pdl_launch_dependents();
   const StepState* st = a.st + a.plan.cta_inst[b];
   if (st->done) return;
   const int pending = st->pending_commit;
@@ -361,21 +363,24 @@ __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualA
   __shared__ int is_last;
   const int b = a.plan.cta_map ? a.plan.cta_map[blockIdx.x] : (int)blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  pdl_launch_dependents();  // as in the primal kernel
+  pdl_launch_dependents();  // the next primal kernel reads the state only after its wait
   const int nt = stage_tiles(a.plan.tiles, a.plan.cta_tile_begin[b], a.plan.cta_tile_begin[b + 1], tl);
-  pdl_wait();
+  // The state this kernel reads was written by the previous dual kernel, which completed
+  // before the primal kernel let this one launch (see there): read it now, from L2 (a line in
+  // this SM's L1 may predate it), so the loads overlap the primal kernel's last CTAs.
   const StepState* st = a.st_mut + a.plan.cta_inst[b];
-  if (st->done) return;
-  const int pending = st->pending_commit;
+  const int done = __ldcg(&st->done);
+  const int pending = __ldcg(&st->pending_commit);
+  const int p = __ldcg(&st->parity);
+  const double commit_weight = __ldcg(&st->commit_weight);
+  const double od64 = __ldcg(&st->omega) * __ldcg(&st->tau);  // primal_weight * step_size
+  pdl_wait();
+  if (done) return;
   const bool commit_only = a.mode == kStepCommitOnly;
   if (commit_only && !pending) return;
   const bool direct = a.direct != 0;
-  __shared__ double s_od;
-  if (threadIdx.x == 0) s_od = st->omega * st->tau;  // primal_weight * step_size
-  __syncthreads();
-  const T w = (T)st->commit_weight;
-  const T od = (T)s_od;
-  const int p = st->parity;
+  const T w = (T)commit_weight;
+  const T od = (T)od64;
   const T* ycur = p ? a.y1 : a.y0;
   T* ynew = p ? a.y0 : a.y1;
   const T* kxcur = p ? a.kx1 : a.kx0;
