@@ -74,17 +74,17 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
   CK(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
   cudaStream_t s = B->stream;
 
-  // pack A and A' (block diagonal), per-instance schedules
-  std::vector<int32_t> arp(M + 1, 0), acol, trp(N + 1, 0), tcol;
-  std::vector<double> aval, tval;
-  acol.reserve(nnz_total); aval.reserve(nnz_total); tcol.reserve(nnz_total); tval.reserve(nnz_total);
+  // pack A (block diagonal) and its per-instance schedules; A' is built from it on the GPU
+  std::vector<int32_t> arp(M + 1, 0), acol;
+  std::vector<double> aval;
+  acol.reserve(nnz_total); aval.reserve(nnz_total);
   std::vector<RowItem> a_items, t_items;
   std::vector<double> l, u, c, b, ol, ou, oc, ob, con, var;
   std::vector<uint8_t> ineq(std::max(M, 1), 0);
   for (int k = 0; k < count; ++k) {
     const gpdhg_lp_desc& d = descs[k];
     const int32_t m = d.num_constraints, n = d.num_variables, ro = B->row_off[k], co = B->col_off[k];
-    const int32_t nnz_a0 = (int32_t)acol.size(), nnz_t0 = (int32_t)tcol.size();
+    const int32_t nnz_a0 = (int32_t)acol.size();
     for (int32_t i = 0; i < m; ++i) {
       for (int32_t e = d.row_ptr[i]; e < d.row_ptr[i + 1]; ++e) {
         acol.push_back(d.col_idx[e] + co);
@@ -93,18 +93,8 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
       arp[ro + i + 1] = (int32_t)acol.size();
       ineq[ro + i] = i >= d.num_equalities;
     }
-    HostCsr t;
-    transpose_csr(m, n, d.row_ptr, d.col_idx, d.values, t);
-    for (int32_t j = 0; j < n; ++j) {
-      for (int32_t e = t.row_ptr[j]; e < t.row_ptr[j + 1]; ++e) {
-        tcol.push_back(t.col[e] + ro);
-        tval.push_back(t.val[e]);
-      }
-      trp[co + j + 1] = (int32_t)tcol.size();
-    }
     for (RowItem it : build_row_items(d.row_ptr, m)) a_items.push_back({it.row_begin + ro, it.row_end + ro, it.group, it.mode, it.nnz_begin + nnz_a0, it.nnz_count});
     if (m == 0) a_items.push_back({ro, ro, 1, kItemStaged, nnz_a0, 0});  // every instance owns a dual CTA: its decision runs there
-    for (RowItem it : build_row_items(t.row_ptr.data(), n)) t_items.push_back({it.row_begin + co, it.row_end + co, it.group, it.mode, it.nnz_begin + nnz_t0, it.nnz_count});
     auto app = [](std::vector<double>& dst, const double* src, const double* fb, int len) {
       const double* p = src ? src : fb;
       if (p) dst.insert(dst.end(), p, p + len);
@@ -162,7 +152,19 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
     if (!it.empty()) CK(cudaMemcpyAsync(dm.items.get(), it.data(), sizeof(RowItem) * it.size(), cudaMemcpyHostToDevice, s));
   };
   up_items(B->A, M, N, arp, acol, aval, a_items);
-  up_items(B->At, N, M, trp, tcol, tval, t_items);
+  // A' of the packed A on the GPU: the transpose of a block-diagonal matrix is block diagonal
+  // with the blocks' transposes in the same order, each the counting sort's (ingest.cu)
+  transpose_on_device(B->A, B->At, s);
+  for (int k = 0; k < count; ++k) {
+    const int32_t co = B->col_off[k], n = B->col_off[k + 1] - co;
+    // the instance's rows of A' from the packed row pointer (absolute nonzero offsets)
+    for (RowItem it : build_row_items(B->At.host_rp.data() + co, n))
+      t_items.push_back({it.row_begin + co, it.row_end + co, it.group, it.mode, it.nnz_begin, it.nnz_count});
+  }
+  B->At.num_items = (int32_t)t_items.size();
+  B->At.items.alloc(std::max<size_t>(t_items.size(), 1));
+  if (!t_items.empty())
+    CK(cudaMemcpyAsync(B->At.items.get(), t_items.data(), sizeof(RowItem) * t_items.size(), cudaMemcpyHostToDevice, s));
   up_i(B->row_off_d, B->row_off);
   up_i(B->neq_d, B->neq);
   up_d(B->l, l); up_d(B->u, u); up_d(B->c, c); up_d(B->b, b);

@@ -2,9 +2,9 @@
 //
 // The reference builds the transpose with CuSparseMatrixCSR(A') (src/cpu_to_gpu.jl:46).
 // Here a stable LSD radix sort of the nonzeros by column (8-bit digits) yields, for every
-// column, its nonzeros in increasing row order, which is exactly the host counting sort's
-// order (transpose_csr): A' is the same matrix entry for entry and in the same storage order,
-// so every SpMV over it sums in the same order as before.
+// column, its nonzeros in increasing row order: the CSR of A' with sorted column indices,
+// the order a counting-sort transpose gives. A block-diagonal A (a packed batch) gives the
+// block diagonal of its blocks' transposes, each exactly what the block alone gives.
 //
 // One pass = a digit histogram per 4,096-key tile, one exclusive scan over (digit, tile), and
 // a scatter in which every tile places its keys in order: per round of 256 keys each warp

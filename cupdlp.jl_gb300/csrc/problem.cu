@@ -41,22 +41,6 @@ std::vector<RowItem> build_row_items(const int32_t* rp, int32_t nrows) {
   return items;
 }
 
-void transpose_csr(int32_t m, int32_t n, const int32_t* rp, const int32_t* col, const double* val, HostCsr& t) {
-  const int64_t nnz = rp[m];
-  t.row_ptr.assign((size_t)n + 1, 0);
-  t.col.resize(nnz);
-  t.val.resize(nnz);
-  for (int64_t k = 0; k < nnz; ++k) t.row_ptr[(size_t)col[k] + 1]++;
-  for (int32_t j = 0; j < n; ++j) t.row_ptr[j + 1] += t.row_ptr[j];
-  std::vector<int32_t> fill(t.row_ptr.begin(), t.row_ptr.end() - 1);
-  for (int32_t i = 0; i < m; ++i)
-    for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
-      const int32_t p = fill[col[k]]++;
-      t.col[p] = i;
-      t.val[p] = val[k];
-    }
-}
-
 namespace {
 
 void upload_csr(DeviceMatrix& dm, int32_t nrows, int32_t ncols, const int32_t* rp, const int32_t* col,

@@ -57,21 +57,14 @@ struct PinnedBuf {
   }
 };
 
-struct HostCsr {
-  std::vector<int32_t> row_ptr, col;
-  std::vector<double> val;
-};
-
 // Row-block schedule: consecutive rows packed while their nonzeros fit the SpMV stage
 // (kStage) and there are at most kBlock of them; a longer row gets an item of its own.
 std::vector<RowItem> build_row_items(const int32_t* row_ptr, int32_t nrows);
 
-// CSR of A' from CSR of A (counting sort, stable in row order).
-void transpose_csr(int32_t m, int32_t n, const int32_t* rp, const int32_t* col, const double* val, HostCsr& out);
-
-// The same A' built on the GPU from an uploaded A (ingest.cu: a stable radix sort by
-// column); fills At's device arrays and its host row pointer. Its row-block schedule is the
-// caller's (set_row_items).
+// CSR of A' built on the GPU from an uploaded A (ingest.cu: a stable radix sort of the
+// nonzeros by column, so each row of A' lists its entries in increasing column of A' = row
+// of A); fills At's device arrays and its host row pointer. Its row-block schedule is the
+// caller's.
 struct DeviceMatrix;
 void transpose_on_device(const DeviceMatrix& A, DeviceMatrix& At, cudaStream_t s);
 
