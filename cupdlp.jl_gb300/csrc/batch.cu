@@ -10,6 +10,9 @@
 // their next evaluation point, evaluates exactly those with segmented FP64 reductions,
 // retires the ones that terminated and re-arms the rest.
 #include <algorithm>
+#include <atomic>
+#include <exception>
+#include <thread>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -47,6 +50,25 @@ void build_seg_items(const std::vector<int32_t>& off, std::vector<SegItem>& item
   if (items.empty()) items.push_back({0, 0, 0});
 }
 
+// Runs f(k) for k in [0, count) on host threads, instances handed out in order from a shared
+// counter; each call writes only instance k's own outputs.
+template <class F>
+void for_each_instance(int count, F f) {
+  const int T = std::max(1, std::min<int>(count, (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
+  if (T == 1) {
+    for (int k = 0; k < count; ++k) f(k);
+    return;
+  }
+  std::atomic<int> next{0};
+  std::vector<std::thread> th;
+  th.reserve(T);
+  for (int t = 0; t < T; ++t)
+    th.emplace_back([&] {
+      for (int k = next++; k < count; k = next++) f(k);
+    });
+  for (auto& x : th) x.join();
+}
+
 void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
   if (count <= 0 || !descs) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "batch needs count > 0 and descriptors");
   B->count = count;
@@ -57,12 +79,27 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
   B->norm_b.assign(count, 0.0);
   B->norm_c.assign(count, 0.0);
   B->neq.resize(count);
+  // every descriptor validated (on host threads, one instance each); the error of the first
+  // invalid instance is the one reported, as a serial loop would
+  {
+    std::vector<std::exception_ptr> err(count);
+    for_each_instance(count, [&](int k) {
+      try {
+        validate_lp_desc(&descs[k], false);
+      } catch (...) {
+        err[k] = std::current_exception();
+      }
+    });
+    for (int k = 0; k < count; ++k)
+      if (err[k]) std::rethrow_exception(err[k]);
+  }
   long long nnz_total = 0;
+  std::vector<long long> nnz_off(count + 1, 0);
   for (int k = 0; k < count; ++k) {
-    validate_lp_desc(&descs[k]);
     B->row_off[k + 1] = B->row_off[k] + descs[k].num_constraints;
     B->col_off[k + 1] = B->col_off[k] + descs[k].num_variables;
     nnz_total += descs[k].nnz;
+    nnz_off[k + 1] = nnz_total;
     B->neq[k] = descs[k].num_equalities;
   }
   if (nnz_total >= (1LL << 31) || (long long)B->row_off[count] >= (1LL << 31) ||
@@ -74,42 +111,43 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
   CK(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
   cudaStream_t s = B->stream;
 
-  // pack A (block diagonal) and its per-instance schedules; A' is built from it on the GPU
-  std::vector<int32_t> arp(M + 1, 0), acol;
-  std::vector<double> aval;
-  acol.reserve(nnz_total); aval.reserve(nnz_total);
-  std::vector<RowItem> a_items, t_items;
-  std::vector<double> l, u, c, b, ol, ou, oc, ob, con, var;
+  // pack A (block diagonal), the vectors, the per-instance schedules and host scalars: each
+  // instance fills its own slices (on host threads); A' is built from A on the GPU
+  std::vector<int32_t> arp(M + 1, 0), acol(nnz_total);
+  std::vector<double> aval(nnz_total);
+  std::vector<double> l(N), u(N), c(N), b(M), ol(N), ou(N), oc(N), ob(M), con(M), var(N);
   std::vector<uint8_t> ineq(std::max(M, 1), 0);
-  for (int k = 0; k < count; ++k) {
+  std::vector<std::vector<RowItem>> a_items_of(count);
+  for_each_instance(count, [&](int k) {
     const gpdhg_lp_desc& d = descs[k];
     const int32_t m = d.num_constraints, n = d.num_variables, ro = B->row_off[k], co = B->col_off[k];
-    const int32_t nnz_a0 = (int32_t)acol.size();
+    const long long z0 = nnz_off[k];
     for (int32_t i = 0; i < m; ++i) {
-      for (int32_t e = d.row_ptr[i]; e < d.row_ptr[i + 1]; ++e) {
-        acol.push_back(d.col_idx[e] + co);
-        aval.push_back(d.values[e]);
-      }
-      arp[ro + i + 1] = (int32_t)acol.size();
+      arp[ro + i + 1] = (int32_t)(z0 + d.row_ptr[i + 1]);
       ineq[ro + i] = i >= d.num_equalities;
     }
-    for (RowItem it : build_row_items(d.row_ptr, m)) a_items.push_back({it.row_begin + ro, it.row_end + ro, it.group, it.mode, it.nnz_begin + nnz_a0, it.nnz_count});
-    if (m == 0) a_items.push_back({ro, ro, 1, kItemStaged, nnz_a0, 0});  // every instance owns a dual CTA: its decision runs there
-    auto app = [](std::vector<double>& dst, const double* src, const double* fb, int len) {
+    for (long long e = 0; e < d.nnz; ++e) {
+      acol[z0 + e] = d.col_idx[e] + co;
+      aval[z0 + e] = d.values[e];
+    }
+    for (RowItem it : build_row_items(d.row_ptr, m))
+      a_items_of[k].push_back({it.row_begin + ro, it.row_end + ro, it.group, it.mode, it.nnz_begin + (int32_t)z0, it.nnz_count});
+    if (m == 0) a_items_of[k].push_back({ro, ro, 1, kItemStaged, (int32_t)z0, 0});  // every instance owns a dual CTA: its decision runs there
+    auto put = [](std::vector<double>& dst, int32_t off, const double* src, const double* fb, int len) {
       const double* p = src ? src : fb;
-      if (p) dst.insert(dst.end(), p, p + len);
-      else dst.insert(dst.end(), len, 1.0);
+      if (p) std::copy(p, p + len, dst.begin() + off);
+      else std::fill(dst.begin() + off, dst.begin() + off + len, 1.0);
     };
-    app(l, d.variable_lower_bound, nullptr, n);
-    app(u, d.variable_upper_bound, nullptr, n);
-    app(c, d.objective_vector, nullptr, n);
-    app(b, d.right_hand_side, nullptr, m);
-    app(ol, d.original_variable_lower_bound, d.variable_lower_bound, n);
-    app(ou, d.original_variable_upper_bound, d.variable_upper_bound, n);
-    app(oc, d.original_objective_vector, d.objective_vector, n);
-    app(ob, d.original_right_hand_side, d.right_hand_side, m);
-    app(con, d.constraint_rescaling, nullptr, m);
-    app(var, d.variable_rescaling, nullptr, n);
+    put(l, co, d.variable_lower_bound, nullptr, n);
+    put(u, co, d.variable_upper_bound, nullptr, n);
+    put(c, co, d.objective_vector, nullptr, n);
+    put(b, ro, d.right_hand_side, nullptr, m);
+    put(ol, co, d.original_variable_lower_bound, d.variable_lower_bound, n);
+    put(ou, co, d.original_variable_upper_bound, d.variable_upper_bound, n);
+    put(oc, co, d.original_objective_vector, d.objective_vector, n);
+    put(ob, ro, d.original_right_hand_side, d.right_hand_side, m);
+    put(con, ro, d.constraint_rescaling, nullptr, m);
+    put(var, co, d.variable_rescaling, nullptr, n);
     // host scalars (as problem_init)
     double amax = 0.0, nb = 0.0, nc = 0.0;
     for (int64_t e = 0; e < d.nnz; ++e) amax = std::max(amax, std::fabs(d.values[e]));
@@ -128,7 +166,9 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
     s2 = 0.0; si = 0.0;
     for (int32_t i = 0; i < m; ++i) { s2 += obb[i] * obb[i]; si = std::max(si, std::fabs(obb[i])); }
     qi.l2_b = std::sqrt(s2); qi.linf_b = si;
-  }
+  });
+  std::vector<RowItem> a_items, t_items;
+  for (auto& v : a_items_of) a_items.insert(a_items.end(), v.begin(), v.end());
 
   auto up_i = [&](DBuf<int32_t>& dst, const std::vector<int32_t>& v) {
     dst.alloc(std::max<size_t>(v.size(), 1));

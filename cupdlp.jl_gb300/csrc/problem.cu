@@ -98,9 +98,9 @@ namespace {
 // The smallest k in [0, len) with bad(k), or -1: contiguous chunks checked on host threads,
 // so the answer (and hence the error reported) is the serial scan's.
 template <class Bad>
-int64_t first_bad(int64_t len, Bad bad) {
+int64_t first_bad(int64_t len, Bad bad, bool threads) {
   const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
-  const int T = (int)std::min<int64_t>(std::min<int64_t>(hw, 32), std::max<int64_t>(1, len / 65536));
+  const int T = threads ? (int)std::min<int64_t>(std::min<int64_t>(hw, 32), std::max<int64_t>(1, len / 65536)) : 1;
   if (T <= 1) {
     for (int64_t k = 0; k < len; ++k)
       if (bad(k)) return k;
@@ -128,7 +128,7 @@ int64_t first_bad(int64_t len, Bad bad) {
 
 // validate (src/preprocess.jl:8-74) for the LP descriptor, plus structural CSR checks
 // the reference gets from SparseMatrixCSC's invariants.
-void validate_lp_desc(const gpdhg_lp_desc* d) {
+void validate_lp_desc(const gpdhg_lp_desc* d, bool threads) {
   if (!d) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "descriptor is NULL");
   if (d->num_variables <= 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "num_variables must be positive");
   if (d->num_constraints < 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "num_constraints must be >= 0");
@@ -139,14 +139,14 @@ void validate_lp_desc(const gpdhg_lp_desc* d) {
     throw Error(GPDHG_ERR_INVALID_ARGUMENT, "required array pointer is NULL");
   const int32_t m = d->num_constraints, n = d->num_variables;
   if (d->row_ptr[0] != 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "row_ptr[0] must be 0");
-  if (first_bad(m, [&](int64_t i) { return d->row_ptr[i + 1] < d->row_ptr[i]; }) >= 0)
+  if (first_bad(m, [&](int64_t i) { return d->row_ptr[i + 1] < d->row_ptr[i]; }, threads) >= 0)
     throw Error(GPDHG_ERR_INVALID_PROBLEM, "row_ptr is not monotone");
   const int64_t nnz = d->row_ptr[m];
   if (nnz != d->nnz) throw Error(GPDHG_ERR_INVALID_PROBLEM, "nnz does not match row_ptr[m]");
   if (nnz > 0 && (!d->col_idx || !d->values)) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "col_idx/values NULL");
   {
     auto bad_col = [&](int64_t k) { return d->col_idx[k] < 0 || d->col_idx[k] >= n; };
-    const int64_t k = first_bad(nnz, [&](int64_t q) { return bad_col(q) || !std::isfinite(d->values[q]); });
+    const int64_t k = first_bad(nnz, [&](int64_t q) { return bad_col(q) || !std::isfinite(d->values[q]); }, threads);
     if (k >= 0) {
       if (bad_col(k)) throw Error(GPDHG_ERR_INVALID_PROBLEM, "column index out of range");
       throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN or Inf found in constraint matrix");
@@ -155,14 +155,14 @@ void validate_lp_desc(const gpdhg_lp_desc* d) {
   auto check_bounds = [&](const double* l, const double* u) {
     const int64_t j = first_bad(n, [&](int64_t q) {
       return l[q] == INFINITY || u[q] == -INFINITY || std::isnan(l[q]) || std::isnan(u[q]);
-    });
+    }, threads);
     if (j < 0) return;
     if (l[j] == INFINITY) throw Error(GPDHG_ERR_INVALID_PROBLEM, "variable_lower_bound contains +Inf");
     if (u[j] == -INFINITY) throw Error(GPDHG_ERR_INVALID_PROBLEM, "variable_upper_bound contains -Inf");
     throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN found in variable bounds");
   };
   auto check_finite = [&](const double* v, int32_t len, const char* what) {
-    if (first_bad(len, [&](int64_t q) { return !std::isfinite(v[q]); }) >= 0)
+    if (first_bad(len, [&](int64_t q) { return !std::isfinite(v[q]); }, threads) >= 0)
       throw Error(GPDHG_ERR_INVALID_PROBLEM, std::string("NaN or Inf found in ") + what);
   };
   check_bounds(d->variable_lower_bound, d->variable_upper_bound);
@@ -174,7 +174,7 @@ void validate_lp_desc(const gpdhg_lp_desc* d) {
   if (d->original_objective_vector) check_finite(d->original_objective_vector, n, "original objective vector");
   if (d->original_right_hand_side && m) check_finite(d->original_right_hand_side, m, "original right hand side");
   auto check_pos = [&](const double* v, int32_t len, const char* what) {
-    if (first_bad(len, [&](int64_t q) { return !(v[q] > 0.0) || !std::isfinite(v[q]); }) >= 0)
+    if (first_bad(len, [&](int64_t q) { return !(v[q] > 0.0) || !std::isfinite(v[q]); }, threads) >= 0)
       throw Error(GPDHG_ERR_INVALID_PROBLEM, std::string(what) + " must be positive and finite");
   };
   if (d->constraint_rescaling && m) check_pos(d->constraint_rescaling, m, "constraint_rescaling");
@@ -182,7 +182,7 @@ void validate_lp_desc(const gpdhg_lp_desc* d) {
 }
 
 void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d) {
-  validate_lp_desc(d);
+  validate_lp_desc(d, true);
   const int32_t m = d->num_constraints, n = d->num_variables;
   p->n = n;
   p->m = m;

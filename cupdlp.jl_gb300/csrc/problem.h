@@ -125,8 +125,10 @@ struct gpdhg_problem {
 };
 
 namespace gpdhg {
-// validate (src/preprocess.jl:8-74) plus CSR structure checks; throws gpdhg::Error.
-void validate_lp_desc(const gpdhg_lp_desc* d);
+// validate (src/preprocess.jl:8-74) plus CSR structure checks; throws gpdhg::Error. The
+// scans of large arrays run on host threads unless threads is false (the first bad entry,
+// and so the error reported, is the serial scan's either way).
+void validate_lp_desc(const gpdhg_lp_desc* d, bool threads);
 // Builds the device problem from a descriptor (throws gpdhg::Error).
 void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d);
 // dst[k] = (float)src[k] on stream s.

@@ -123,7 +123,7 @@ class Server {
   }
 
   uint64_t submit(const gpdhg_lp_desc& d, const gpdhg_params& p) {
-    validate_lp_desc(&d);
+    validate_lp_desc(&d, true);
     auto r = std::make_shared<Request>();
     r->params = p;
     r->footprint = footprint_bytes(d, p);
