@@ -167,6 +167,34 @@ gpdhg_status gpdhg_problem_create_unscaled(const gpdhg_lp_desc* desc, const gpdh
   });
 }
 
+gpdhg_status gpdhg_problem_create_csc(const gpdhg_lp_desc* desc, const int64_t* col_ptr, const int64_t* row_val,
+                                      const double* nz_val, int32_t index_base, const gpdhg_params* unscaled_params,
+                                      gpdhg_problem** out) {
+  return guarded([&] {
+    if (!out) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (!desc) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "desc is NULL");
+    if (unscaled_params) {
+      if (desc->original_variable_lower_bound || desc->original_variable_upper_bound ||
+          desc->original_objective_vector || desc->original_right_hand_side || desc->constraint_rescaling ||
+          desc->variable_rescaling)
+        throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT,
+                           "an unscaled descriptor carries no original_* or rescaling vectors");
+      if (unscaled_params->l_inf_ruiz_iterations < 0)
+        throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "l_inf_ruiz_iterations must be >= 0");
+    }
+    gpdhg_problem* p = new gpdhg_problem();
+    try {
+      gpdhg::problem_init_csc(p, desc, col_ptr, row_val, nz_val, index_base);
+      if (unscaled_params) gpdhg::rescale_on_device(p, *unscaled_params);
+    } catch (...) {
+      delete p;
+      throw;
+    }
+    *out = p;
+  });
+}
+
 gpdhg_status gpdhg_get_rescaling(const gpdhg_problem* p, double* constraint_rescaling, double* variable_rescaling) {
   return guarded([&] {
     if (!p) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "problem is NULL");

@@ -126,32 +126,22 @@ int64_t first_bad(int64_t len, Bad bad, bool threads) {
 
 }  // namespace
 
-// validate (src/preprocess.jl:8-74) for the LP descriptor, plus structural CSR checks
-// the reference gets from SparseMatrixCSC's invariants.
-void validate_lp_desc(const gpdhg_lp_desc* d, bool threads) {
+namespace {
+
+// The descriptor's dimensions and vectors (validate, src/preprocess.jl:8-74, without the matrix).
+void validate_dims(const gpdhg_lp_desc* d) {
   if (!d) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "descriptor is NULL");
   if (d->num_variables <= 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "num_variables must be positive");
   if (d->num_constraints < 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "num_constraints must be >= 0");
   if (d->num_equalities < 0 || d->num_equalities > d->num_constraints)
     throw Error(GPDHG_ERR_INVALID_PROBLEM, "num_equalities out of [0, num_constraints]");
-  if (!d->row_ptr || !d->variable_lower_bound || !d->variable_upper_bound || !d->objective_vector ||
+  if (!d->variable_lower_bound || !d->variable_upper_bound || !d->objective_vector ||
       (d->num_constraints > 0 && !d->right_hand_side))
     throw Error(GPDHG_ERR_INVALID_ARGUMENT, "required array pointer is NULL");
+}
+
+void validate_vectors(const gpdhg_lp_desc* d, bool threads) {
   const int32_t m = d->num_constraints, n = d->num_variables;
-  if (d->row_ptr[0] != 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "row_ptr[0] must be 0");
-  if (first_bad(m, [&](int64_t i) { return d->row_ptr[i + 1] < d->row_ptr[i]; }, threads) >= 0)
-    throw Error(GPDHG_ERR_INVALID_PROBLEM, "row_ptr is not monotone");
-  const int64_t nnz = d->row_ptr[m];
-  if (nnz != d->nnz) throw Error(GPDHG_ERR_INVALID_PROBLEM, "nnz does not match row_ptr[m]");
-  if (nnz > 0 && (!d->col_idx || !d->values)) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "col_idx/values NULL");
-  {
-    auto bad_col = [&](int64_t k) { return d->col_idx[k] < 0 || d->col_idx[k] >= n; };
-    const int64_t k = first_bad(nnz, [&](int64_t q) { return bad_col(q) || !std::isfinite(d->values[q]); }, threads);
-    if (k >= 0) {
-      if (bad_col(k)) throw Error(GPDHG_ERR_INVALID_PROBLEM, "column index out of range");
-      throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN or Inf found in constraint matrix");
-    }
-  }
   auto check_bounds = [&](const double* l, const double* u) {
     const int64_t j = first_bad(n, [&](int64_t q) {
       return l[q] == INFINITY || u[q] == -INFINITY || std::isnan(l[q]) || std::isnan(u[q]);
@@ -181,8 +171,38 @@ void validate_lp_desc(const gpdhg_lp_desc* d, bool threads) {
   if (d->variable_rescaling) check_pos(d->variable_rescaling, n, "variable_rescaling");
 }
 
-void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d) {
-  validate_lp_desc(d, true);
+}  // namespace
+
+// validate (src/preprocess.jl:8-74) for the LP descriptor, plus structural CSR checks
+// the reference gets from SparseMatrixCSC's invariants.
+void validate_lp_desc(const gpdhg_lp_desc* d, bool threads) {
+  validate_dims(d);
+  if (!d->row_ptr) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "required array pointer is NULL");
+  const int32_t m = d->num_constraints, n = d->num_variables;
+  if (d->row_ptr[0] != 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "row_ptr[0] must be 0");
+  if (first_bad(m, [&](int64_t i) { return d->row_ptr[i + 1] < d->row_ptr[i]; }, threads) >= 0)
+    throw Error(GPDHG_ERR_INVALID_PROBLEM, "row_ptr is not monotone");
+  const int64_t nnz = d->row_ptr[m];
+  if (nnz != d->nnz) throw Error(GPDHG_ERR_INVALID_PROBLEM, "nnz does not match row_ptr[m]");
+  if (nnz > 0 && (!d->col_idx || !d->values)) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "col_idx/values NULL");
+  {
+    auto bad_col = [&](int64_t k) { return d->col_idx[k] < 0 || d->col_idx[k] >= n; };
+    const int64_t k = first_bad(nnz, [&](int64_t q) { return bad_col(q) || !std::isfinite(d->values[q]); }, threads);
+    if (k >= 0) {
+      if (bad_col(k)) throw Error(GPDHG_ERR_INVALID_PROBLEM, "column index out of range");
+      throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN or Inf found in constraint matrix");
+    }
+  }
+  validate_vectors(d, threads);
+}
+
+namespace {
+
+// The part of problem creation after validation: build(s) uploads one of the two CSR copies
+// and builds the other on the device; meanwhile a helper thread forms the host scalars
+// (serial sums) from the matrix values and the vectors.
+template <class Build>
+void init_with(gpdhg_problem* p, const gpdhg_lp_desc* d, const double* values, Build build) {
   const int32_t m = d->num_constraints, n = d->num_variables;
   p->n = n;
   p->m = m;
@@ -191,11 +211,10 @@ void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d) {
   p->obj_const = d->objective_constant;
   CK(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
   cudaStream_t s = p->stream;
-
-  // host scalars on a helper thread while the device builds A' (serial sums, as before)
-  std::thread scalars([p, d, m, n] {
+  const int64_t nnz = d->nnz;
+  std::thread scalars([p, d, m, n, values, nnz] {
     double amax = 0.0;
-    for (int64_t k = 0; k < d->nnz; ++k) amax = std::max(amax, std::fabs(d->values[k]));
+    for (int64_t k = 0; k < nnz; ++k) amax = std::max(amax, std::fabs(values[k]));
     p->amax = amax;
     p->norm2_c_scaled = norm2(d->objective_vector, n);
     p->norm2_b_scaled = m ? norm2(d->right_hand_side, m) : 0.0;
@@ -207,8 +226,7 @@ void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d) {
     p->l2_b = m ? norm2(ob, m) : 0.0;
   });
   try {
-    upload_csr(p->A, m, n, d->row_ptr, d->col_idx, d->values, s);
-    transpose_on_device(p->A, p->At, s);
+    build(s);
     std::vector<double> ones((size_t)std::max(m, n), 1.0);
     upload_vec(p->l, d->variable_lower_bound, n, s);
     upload_vec(p->u, d->variable_upper_bound, n, s);
@@ -228,6 +246,62 @@ void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d) {
   }
   scalars.join();
   CK(cudaStreamSynchronize(s));
+}
+
+// dst[k] = (int32_t)(src[k] - base) on host threads
+void narrow_indices(const int64_t* src, int64_t len, int64_t base, std::vector<int32_t>& dst) {
+  dst.resize((size_t)len);
+  const int T = (int)std::max<int64_t>(1, std::min<int64_t>(std::min(16u, std::max(1u, std::thread::hardware_concurrency())), len / 65536));
+  std::vector<std::thread> th;
+  for (int t = 0; t < T; ++t)
+    th.emplace_back([&, t] {
+      for (int64_t k = len * t / T; k < len * (t + 1) / T; ++k) dst[(size_t)k] = (int32_t)(src[k] - base);
+    });
+  for (auto& x : th) x.join();
+}
+
+}  // namespace
+
+void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d) {
+  validate_lp_desc(d, true);
+  init_with(p, d, d->values, [&](cudaStream_t s) {
+    upload_csr(p->A, d->num_constraints, d->num_variables, d->row_ptr, d->col_idx, d->values, s);
+    transpose_on_device(p->A, p->At, s);
+  });
+}
+
+void problem_init_csc(gpdhg_problem* p, const gpdhg_lp_desc* d, const int64_t* col_ptr, const int64_t* row_val,
+                      const double* nz_val, int32_t base) {
+  validate_dims(d);
+  if (d->row_ptr || d->col_idx || d->values)
+    throw Error(GPDHG_ERR_INVALID_ARGUMENT, "a CSC descriptor carries no row_ptr, col_idx or values");
+  if (base != 0 && base != 1) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "index_base must be 0 or 1");
+  if (!col_ptr) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "col_ptr is NULL");
+  const int32_t m = d->num_constraints, n = d->num_variables;
+  if (col_ptr[0] != base) throw Error(GPDHG_ERR_INVALID_PROBLEM, "col_ptr[0] must be index_base");
+  if (first_bad(n, [&](int64_t j) { return col_ptr[j + 1] < col_ptr[j]; }, true) >= 0)
+    throw Error(GPDHG_ERR_INVALID_PROBLEM, "col_ptr is not monotone");
+  const int64_t nnz = col_ptr[n] - base;
+  if (nnz != d->nnz) throw Error(GPDHG_ERR_INVALID_PROBLEM, "nnz does not match col_ptr[n] - index_base");
+  if (nnz >= (1LL << 31)) throw Error(GPDHG_ERR_INVALID_PROBLEM, "more than 2^31 - 1 nonzeros");
+  if (nnz > 0 && (!row_val || !nz_val)) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "row_val/nz_val NULL");
+  {
+    auto bad_row = [&](int64_t k) { return row_val[k] < base || row_val[k] >= (int64_t)m + base; };
+    const int64_t k = first_bad(nnz, [&](int64_t q) { return bad_row(q) || !std::isfinite(nz_val[q]); }, true);
+    if (k >= 0) {
+      if (bad_row(k)) throw Error(GPDHG_ERR_INVALID_PROBLEM, "row index out of range");
+      throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN or Inf found in constraint matrix");
+    }
+  }
+  validate_vectors(d, true);
+  init_with(p, d, nz_val, [&](cudaStream_t s) {
+    // CSC(A) read as CSR(A'): its pointers become A's row pointer after the device transpose
+    std::vector<int32_t> rp, ri;
+    narrow_indices(col_ptr, (int64_t)n + 1, base, rp);
+    narrow_indices(row_val, nnz, base, ri);
+    upload_csr(p->At, n, m, rp.data(), ri.data(), nz_val, s);
+    transpose_on_device(p->At, p->A, s);
+  });
 }
 
 void ensure_fp32_values(gpdhg_problem* p) {

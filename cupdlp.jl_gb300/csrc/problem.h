@@ -131,6 +131,10 @@ namespace gpdhg {
 void validate_lp_desc(const gpdhg_lp_desc* d, bool threads);
 // Builds the device problem from a descriptor (throws gpdhg::Error).
 void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d);
+// The same from the matrix in compressed sparse columns (index base 0 or 1, int64 indices, as
+// Julia's SparseMatrixCSC): CSC(A) is uploaded as CSR(A') and A is built on the device.
+void problem_init_csc(gpdhg_problem* p, const gpdhg_lp_desc* d, const int64_t* col_ptr, const int64_t* row_val,
+                      const double* nz_val, int32_t base);
 // dst[k] = (float)src[k] on stream s.
 void launch_convert_d2f(const double* src, float* dst, long long n, cudaStream_t s);
 // dst[k] = 1 / src[k] on stream s.

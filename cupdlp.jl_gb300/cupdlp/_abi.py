@@ -38,6 +38,7 @@ PRECISION_FP32 = 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
+_lp = C.POINTER(C.c_int64)
 
 
 class Params(C.Structure):
@@ -178,6 +179,8 @@ SIGNATURES = {
     "gpdhg_problem_create_unscaled": (C.c_int, [C.POINTER(LpDesc), C.POINTER(Params),
                                                 C.POINTER(C.c_void_p)]),
     "gpdhg_get_rescaling": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "gpdhg_problem_create_csc": (C.c_int, [C.POINTER(LpDesc), _lp, _lp, _dp, C.c_int32, C.POINTER(Params),
+                                           C.POINTER(C.c_void_p)]),
     "gpdhg_solve": (C.c_int, [C.c_void_p, C.POINTER(Params), C.POINTER(Result), _dp, _dp]),
     "gpdhg_get_stats": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(IterationStats)]),
     "gpdhg_set_warm_start": (C.c_int, [C.c_void_p, _dp, _dp]),
@@ -238,6 +241,13 @@ def check(status: int, lib=None) -> None:
         lib = lib or _lib
         msg = lib.gpdhg_last_error().decode() if lib is not None else ""
         raise GpdhgError(status, msg)
+
+
+def lptr(a):
+    """int64_t* of a contiguous int64 numpy array (or NULL for None)."""
+    if a is None:
+        return C.cast(None, _lp)
+    return a.ctypes.data_as(_lp)
 
 
 def dptr(a):

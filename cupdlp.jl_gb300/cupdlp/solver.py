@@ -88,6 +88,33 @@ class DeviceProblem:
         self.handle = h
 
     @classmethod
+    def from_csc(cls, desc: _Desc, a_csc, index_base: int = 0, unscaled_params: Optional[PdhgParameters] = None,
+                 lib=None):
+        """gpdhg_problem_create_csc: the matrix as compressed sparse columns (scipy's csc
+        indptr / indices / data, or Julia's 1-based colptr / rowval / nzval with index_base 1);
+        `desc` supplies the vectors (its CSR arrays are not read). With unscaled_params the
+        data are unscaled and rescaled on the GPU."""
+        self = cls.__new__(cls)
+        self.lib = lib or _abi.load()
+        self.n, self.m = desc.desc.num_variables, desc.desc.num_constraints
+        colptr = np.ascontiguousarray(a_csc.indptr, dtype=np.int64) + index_base
+        rowval = np.ascontiguousarray(a_csc.indices, dtype=np.int64) + index_base
+        nzval = np.ascontiguousarray(a_csc.data, dtype=np.float64)
+        d = _abi.LpDesc()
+        C.pointer(d)[0] = desc.desc
+        d.row_ptr = C.cast(None, _abi._ip)
+        d.col_idx = C.cast(None, _abi._ip)
+        d.values = C.cast(None, _abi._dp)
+        d.nnz = int(nzval.size)
+        cp = params_to_c(unscaled_params) if unscaled_params is not None else None
+        h = C.c_void_p()
+        _abi.check(self.lib.gpdhg_problem_create_csc(C.byref(d), _abi.lptr(colptr), _abi.lptr(rowval),
+                                                     _abi.dptr(nzval), int(index_base),
+                                                     C.byref(cp) if cp is not None else None, C.byref(h)), self.lib)
+        self.handle = h
+        return self
+
+    @classmethod
     def from_unscaled(cls, p: QuadraticProgrammingProblem, params: PdhgParameters, lib=None):
         """Rescaling on the GPU (gpdhg_problem_create_unscaled)."""
         self = cls.__new__(cls)

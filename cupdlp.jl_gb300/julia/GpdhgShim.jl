@@ -185,20 +185,22 @@ function solve(params, scaled_problem; precision::Integer = 0)
     s = scaled_problem.scaled_qp
     o = scaled_problem.original_qp
     m, n = size(s.constraint_matrix)
-    # CSC (1-based, Int64) -> CSR (0-based, Int32): the CSC of A' is the CSR of A
-    At = SparseArrays.sparse(transpose(s.constraint_matrix))
-    row_ptr = Int32.(At.colptr .- 1)
-    col_idx = Int32.(At.rowval .- 1)
-    values = Vector{Float64}(At.nzval)
-    arrays = (row_ptr, col_idx, values, s.variable_lower_bound, s.variable_upper_bound, s.objective_vector,
+    # The SparseMatrixCSC goes in as it is (1-based, Int64 indices): gpdhg_problem_create_csc
+    # uploads it as CSR(A') and builds CSR(A) on the GPU. `convert` copies only when the index
+    # type is not Int64 already.
+    A = s.constraint_matrix
+    colptr = convert(Vector{Int64}, A.colptr)
+    rowval = convert(Vector{Int64}, A.rowval)
+    nzval = convert(Vector{Float64}, A.nzval)
+    arrays = (colptr, rowval, nzval, s.variable_lower_bound, s.variable_upper_bound, s.objective_vector,
               s.right_hand_side, o.variable_lower_bound, o.variable_upper_bound, o.objective_vector,
               o.right_hand_side, scaled_problem.constraint_rescaling, scaled_problem.variable_rescaling)
     avg_primal = zeros(n)
     avg_dual = zeros(m)
     result = Ref{GpdhgResult}()
     GC.@preserve arrays avg_primal avg_dual begin
-        desc = Ref(GpdhgLpDesc(Int32(n), Int32(m), Int32(s.num_equalities), Int32(0), Int64(length(values)),
-                               pointer(row_ptr), pointer(col_idx), pointer(values),
+        desc = Ref(GpdhgLpDesc(Int32(n), Int32(m), Int32(s.num_equalities), Int32(0), Int64(length(nzval)),
+                               Ptr{Int32}(C_NULL), Ptr{Int32}(C_NULL), Ptr{Float64}(C_NULL),
                                pointer(s.variable_lower_bound), pointer(s.variable_upper_bound),
                                pointer(s.objective_vector), pointer(s.right_hand_side), s.objective_constant,
                                pointer(o.variable_lower_bound), pointer(o.variable_upper_bound),
@@ -206,7 +208,9 @@ function solve(params, scaled_problem; precision::Integer = 0)
                                pointer(scaled_problem.constraint_rescaling),
                                pointer(scaled_problem.variable_rescaling)))
         handle = Ref{Ptr{Cvoid}}(C_NULL)
-        check(ccall((:gpdhg_problem_create, libgpdhg), Cint, (Ref{GpdhgLpDesc}, Ref{Ptr{Cvoid}}), desc, handle))
+        check(ccall((:gpdhg_problem_create_csc, libgpdhg), Cint,
+                    (Ref{GpdhgLpDesc}, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Int32, Ptr{Cvoid}, Ref{Ptr{Cvoid}}),
+                    desc, colptr, rowval, nzval, Int32(1), C_NULL, handle))
         try
             cp = Ref(c_params(params, precision))
             check(ccall((:gpdhg_solve, libgpdhg), Cint,

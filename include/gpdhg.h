@@ -275,6 +275,21 @@ gpdhg_status gpdhg_get_rescaling(const gpdhg_problem* p, double* constraint_resc
                                  double* variable_rescaling);
 
 /*
+ * The constraint matrix in compressed sparse COLUMNS, as Julia's SparseMatrixCSC holds it
+ * (col_ptr: n+1, row_val: nnz, nz_val: nnz; index_base 1 for Julia's 1-based arrays, 0 for
+ * 0-based ones). CSC(A) is CSR(A^T): the library uploads it as A^T and builds A on the
+ * device (src/cpu_to_gpu.jl:45-46 builds the CSR copies from the CSC on the host). `desc`
+ * gives the dimensions, nnz and the vectors; its row_ptr, col_idx and values must be NULL.
+ * With `unscaled_params` NULL the data are the scaled problem, as for gpdhg_problem_create;
+ * otherwise they are unscaled and rescaled on the device as by gpdhg_problem_create_unscaled
+ * (then `desc` carries no original_* or rescaling vectors). For a CSC whose row indices
+ * increase within each column the handle is the one the CSR of the same matrix gives.
+ */
+gpdhg_status gpdhg_problem_create_csc(const gpdhg_lp_desc* desc, const int64_t* col_ptr, const int64_t* row_val,
+                                      const double* nz_val, int32_t index_base, const gpdhg_params* unscaled_params,
+                                      gpdhg_problem** out);
+
+/*
  * Runs the restarted PDHG loop of optimize() (src/primal_dual_hybrid_gradient_gpu.jl:
  * 494-797) on the handle's problem from a zero starting point (or the warm start set
  * with gpdhg_set_warm_start). On return `primal_out` (n) and `dual_out` (m) hold the

@@ -118,3 +118,40 @@ def test_server_footprint_and_null_handling():
     assert lib.gpdhg_server_poll(None, 1, None, None, None) == _abi.ERR_INVALID_ARGUMENT
     assert lib.gpdhg_server_wait(None, 1, 0.0, None, None, None) == _abi.ERR_INVALID_ARGUMENT
     assert lib.gpdhg_server_create(None, None) == _abi.ERR_INVALID_ARGUMENT
+
+
+def _csc_err(lib, p, mutate=None, base=0, keep_csr=False):
+    """gpdhg_problem_create_csc on problem p, after mutate(colptr, rowval, nzval)."""
+    d = unscaled_desc(p)
+    a = p.constraint_matrix.tocsc()
+    colptr = np.ascontiguousarray(a.indptr, dtype=np.int64) + base
+    rowval = np.ascontiguousarray(a.indices, dtype=np.int64) + base
+    nzval = np.ascontiguousarray(a.data, dtype=np.float64)
+    if mutate:
+        mutate(colptr, rowval, nzval)
+    desc = _abi.LpDesc()
+    C.pointer(desc)[0] = d.desc
+    if not keep_csr:
+        desc.row_ptr = C.cast(None, _abi._ip)
+        desc.col_idx = C.cast(None, _abi._ip)
+        desc.values = C.cast(None, _abi._dp)
+    h = C.c_void_p()
+    st = lib.gpdhg_problem_create_csc(C.byref(desc), _abi.lptr(colptr), _abi.lptr(rowval), _abi.dptr(nzval), base,
+                                      None, C.byref(h))
+    return st, lib.gpdhg_last_error().decode()
+
+
+def test_csc_entry_rejects_bad_input_before_any_gpu_work(lib):
+    p, _ = instances.tiny()
+    st, msg = _csc_err(lib, p, base=2)
+    assert st == _abi.ERR_INVALID_ARGUMENT and "index_base" in msg
+    st, msg = _csc_err(lib, p, keep_csr=True)
+    assert st == _abi.ERR_INVALID_ARGUMENT and "CSC descriptor" in msg
+    st, msg = _csc_err(lib, p, base=1, mutate=lambda cp, rv, nz: cp.__setitem__(0, 0))
+    assert st == _abi.ERR_INVALID_PROBLEM and "col_ptr[0]" in msg
+    st, msg = _csc_err(lib, p, base=1, mutate=lambda cp, rv, nz: rv.__setitem__(0, 0))
+    assert st == _abi.ERR_INVALID_PROBLEM and "row index" in msg
+    st, msg = _csc_err(lib, p, mutate=lambda cp, rv, nz: nz.__setitem__(0, np.inf))
+    assert st == _abi.ERR_INVALID_PROBLEM and "constraint matrix" in msg
+    st, msg = _csc_err(lib, p, mutate=lambda cp, rv, nz: cp.__setitem__(-1, cp[-1] + 1))
+    assert st == _abi.ERR_INVALID_PROBLEM and "nnz" in msg
