@@ -90,9 +90,9 @@ def bytes_model(m, n, nnz, prec):
     mat_t = (sv + si) * nnz + si * (n + 1)   # CSR of A' (n rows)
     mat_a = (sv + si) * nnz + si * (m + 1)   # CSR of A (m rows)
     return {
-        # primal kernel with a commit: A' stream, gather y, read x dx c l u sx skty,
-        # write x dx kty sx skty
-        "primal_commit": mat_t + sx * m + 12 * sx * n,
+        # primal kernel with a commit: A' stream, gather y, read x dx c l u sx,
+        # write x dx kty sx
+        "primal_commit": mat_t + sx * m + 10 * sx * n,
         # primal kernel after a rejection: read x kty c l u, write dx
         "primal_plain": 6 * sx * n,
         # dual kernel: A stream, gather dx, read y kx b, write y' kx'

@@ -21,6 +21,7 @@
 
 #include "batch.h"
 #include "batch_kernels.cuh"
+#include "spmv.cuh"
 #include "tiles.h"
 #include "host_logic.h"
 
@@ -240,7 +241,7 @@ struct BatchWorkspace {
   int count, N, M;
   DBuf<T> l_own, u_own, c_own, b_own, Aval32, Atval32;
   const T *l, *u, *c, *b;
-  DBuf<T> x, dx, kty, sx, skty, ax, agrad, grad, rx, rgrad;
+  DBuf<T> x, dx, kty, sx, ax, agrad, grad, rx, rgrad, aty;
   DBuf<T> y0, y1, kx0, kx1, sy, skx, ay, akx, ry, rkx;
   DBuf<StepState> st_dev;
   PinnedBuf<StepState> st_host;
@@ -293,7 +294,7 @@ struct BatchWorkspace {
         }
       }
     }
-    alloc_all<T>({&x, &dx, &kty, &sx, &skty, &ax, &agrad, &grad, &rx, &rgrad}, N);
+    alloc_all<T>({&x, &dx, &kty, &sx, &ax, &agrad, &grad, &rx, &rgrad, &aty}, N);
     alloc_all<T>({&y0, &y1, &kx0, &kx1, &sy, &skx, &ay, &akx, &ry, &rkx}, M);
     rvar.alloc(std::max(N, 1));
     rcon.alloc(std::max(M, 1));
@@ -369,7 +370,7 @@ struct BatchWorkspace {
   }
   PrimalArgs<T> pargs(int mode) {
     return PrimalArgs<T>{B->At.view<T>(), view_p(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(),
-                         skty.get(), y0.get(), y1.get(), st_dev.get(), part_p.get(), part_p_split.get(), mode, direct};
+                         y0.get(), y1.get(), st_dev.get(), part_p.get(), part_p_split.get(), mode, direct};
   }
   DualArgs<T> dargs(int mode) {
     return DualArgs<T>{B->A.view<T>(), view_d(), plan_p.inst_cta_begin.get(), plan_p.inst_split_begin.get(),
@@ -442,7 +443,7 @@ static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& 
   const long long launches0 = W.launches;
   if (W.grid_p != W.plan_p.num_ctas) W.compact(std::vector<char>(K, 0));  // a new solve: every instance runs
   // initial state (:494-611) for every instance
-  for (DBuf<T>* v : {&W.x, &W.kty, &W.sx, &W.skty, &W.dx, &W.ax, &W.agrad, &W.rx})
+  for (DBuf<T>* v : {&W.x, &W.kty, &W.sx, &W.dx, &W.ax, &W.agrad, &W.rx})
     CK(cudaMemsetAsync(v->get(), 0, sizeof(T) * v->n, s));
   for (DBuf<T>* v : {&W.y0, &W.y1, &W.kx0, &W.kx1, &W.sy, &W.skx, &W.ay, &W.akx, &W.ry, &W.rkx})
     CK(cudaMemsetAsync(v->get(), 0, sizeof(T) * v->n, s));
@@ -501,17 +502,24 @@ static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& 
       CK_LAUNCH();
       for (int k = 0; k < K; ++k)
         if (fh[k]) st[k].pending_commit = 0;
-      batch_average_n_kernel<T><<<W.grid(N), kBlock, 0, s>>>(W.vn(W.active()), W.use_current(), W.sx.get(),
-                                                             W.skty.get(), W.c, W.x.get(), W.grad.get(), W.ax.get(),
-                                                             W.agrad.get());
-      CK_LAUNCH();
+      // y-bar first, then the averages' K'y = A' y-bar of the instances evaluated now (as the
+      // lone solve forms it), then x-bar and the average gradient
       if (M) {
         batch_average_m_kernel<T><<<W.grid(M), kBlock, 0, s>>>(W.vm(W.active()), W.use_current(), W.sy.get(),
                                                                W.skx.get(), W.y0.get(), W.y1.get(), W.kx0.get(),
                                                                W.kx1.get(), W.ay.get(), W.akx.get());
         CK_LAUNCH();
       }
-      W.launches += 2;
+      if (B->At.num_items > 0) {
+        spmv_kernel<T><<<B->At.num_items, kBlock, 0, s>>>(B->At.view<T>(), W.ay.get(), W.aty.get(), B->col_inst.get(),
+                                                          W.active());
+        CK_LAUNCH();
+      }
+      batch_average_n_kernel<T><<<W.grid(N), kBlock, 0, s>>>(W.vn(W.active()), W.use_current(), W.sx.get(),
+                                                             W.aty.get(), W.c, W.x.get(), W.grad.get(), W.ax.get(),
+                                                             W.agrad.get());
+      CK_LAUNCH();
+      W.launches += 3;
       W.template seg_reduce<kEvalNQ, kEvalNMax>(
           true, EvalN<T>{W.ax.get(), W.agrad.get(), B->var.get(), W.rvar.get(), B->ol.get(), B->ou.get(), B->oc.get()},
           0);
@@ -630,8 +638,7 @@ static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& 
           W.push_state();  // restart kernels read each instance's parity
           batch_restart_n_kernel<T><<<W.grid(N), kBlock, 0, s>>>(W.vn(W.active()), W.to_avg(), W.ax.get(),
                                                                  W.agrad.get(), W.c, W.x.get(), W.kty.get(),
-                                                                 W.grad.get(), W.sx.get(), W.skty.get(), W.rx.get(),
-                                                                 W.rgrad.get());
+                                                                 W.grad.get(), W.sx.get(), W.rx.get(), W.rgrad.get());
           CK_LAUNCH();
           if (M) {
             batch_restart_m_kernel<T><<<W.grid(M), kBlock, 0, s>>>(W.vm(W.active()), W.to_avg(), W.ay.get(),

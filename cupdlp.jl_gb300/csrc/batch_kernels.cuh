@@ -64,9 +64,10 @@ struct BatchVecArgs {
   int len;
 };
 
-// compute_average! (or the current point when the instance has no average yet)
+// compute_average! (or the current point when the instance has no average yet), the average's
+// K'y given as aty = A' y-bar
 template <class T>
-__global__ void batch_average_n_kernel(BatchVecArgs<T> v, const uint8_t* use_current, const T* sx, const T* skty,
+__global__ void batch_average_n_kernel(BatchVecArgs<T> v, const uint8_t* use_current, const T* sx, const T* aty,
                                        const T* c, const T* x, const T* grad, T* ax, T* agrad) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < v.len; j += gridDim.x * blockDim.x) {
     const int k = v.inst_of[j];
@@ -77,8 +78,7 @@ __global__ void batch_average_n_kernel(BatchVecArgs<T> v, const uint8_t* use_cur
     } else {
       const StepState& q = v.st[k];
       ax[j] = (T)div_rcp((double)sx[j], q.sum_w_primal, q.rcp_w_primal);
-      const T g = (T)(-div_rcp((double)skty[j], q.sum_w_dual, q.rcp_w_dual));
-      agrad[j] = g + c[j];
+      agrad[j] = c[j] - aty[j];  // aty = A' y-bar
     }
   }
 }
@@ -113,7 +113,7 @@ __global__ void batch_grad_kernel(BatchVecArgs<T> v, const T* c, const T* kty, T
 // to_avg[k] selects reset-to-average; sums are cleared; the restart point is stored.
 template <class T>
 __global__ void batch_restart_n_kernel(BatchVecArgs<T> v, const uint8_t* to_avg, const T* ax, const T* agrad,
-                                       const T* c, T* x, T* kty, T* grad, T* sx, T* skty, T* rx, T* rgrad) {
+                                       const T* c, T* x, T* kty, T* grad, T* sx, T* rx, T* rgrad) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < v.len; j += gridDim.x * blockDim.x) {
     const int k = v.inst_of[j];
     if (!v.flag[k]) continue;
@@ -123,7 +123,6 @@ __global__ void batch_restart_n_kernel(BatchVecArgs<T> v, const uint8_t* to_avg,
       grad[j] = agrad[j];
     }
     sx[j] = T(0);
-    skty[j] = T(0);
     rx[j] = x[j];
     rgrad[j] = grad[j];
   }

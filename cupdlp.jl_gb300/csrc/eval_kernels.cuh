@@ -274,7 +274,8 @@ struct KktM {
 };
 
 // One evaluation's column pass (optimize(), src/primal_dual_hybrid_gradient_gpu.jl:633-760):
-// the average (compute_average!, src/saddle_point_gpu.jl:226-240; or the current point when
+// the average (compute_average!, src/saddle_point_gpu.jl:226-240, with the average's K'y
+// given as aty = A' y-bar, computed after the row pass formed y-bar; or the current point when
 // there is none, which takes the gradient buffer as it stood), its unscaled statistics
 // (EvalN), buffer_primal_gradient = c - K'y (:742), and the KKT ingredients of the current,
 // average and last-restart points (KktN). The last restart point's ingredients depend on
@@ -282,10 +283,10 @@ struct KktM {
 // Per element the arithmetic is that of the separate kernels, so the sums are the same.
 template <class T>
 struct EvalPassN {
-  EvalN<T> en;   // its ax / agrad are not read: the average comes from sx / skty here
+  EvalN<T> en;   // its ax / agrad are not read: the average comes from sx and aty here
   KktN<T> kn;    // kn.x0 = x, kn.x2 = rx, kn.g2 = rgrad
   const T* sx;
-  const T* skty;
+  const T* aty;  // A' y-bar
   const T* kty;
   T* ax;         // the average, written
   T* agrad;
@@ -303,8 +304,7 @@ struct EvalPassN {
       ga = gold;
     } else {
       xa = (T)div_rcp((double)sx[j], wx, rwx);
-      const T g = (T)(-div_rcp((double)skty[j], wy, rwy));
-      ga = g + c;
+      ga = c - aty[j];
     }
     ax[j] = xa;
     agrad[j] = ga;

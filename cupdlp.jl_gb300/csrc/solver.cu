@@ -53,18 +53,6 @@ void launch_reciprocal(const double* src, double* dst, long long n, cudaStream_t
   CK_LAUNCH();
 }
 
-// Plain y = M x (warm start, power method, FP64 hand-off).
-struct NoPre {};
-template <class T>
-__global__ void __launch_bounds__(kBlock) spmv_kernel(CsrView<T> M, const T* __restrict__ x, T* y) {
-  __shared__ T stage[kStage];
-  __shared__ T stage2[sizeof(T) == 8 ? kStage : 1];
-  __shared__ T wsum[kBlock / 32];
-  auto pre = [](int) { return NoPre{}; };
-  auto post = [&](int i, T s, const NoPre&) { y[i] = s; };
-  if ((int)blockIdx.x < M.num_items) spmv_item(M, x, blockIdx.x, stage, stage2, wsum, pre, post);
-}
-
 template <class T>
 struct DotF {
   const T* a;
@@ -121,7 +109,7 @@ struct Workspace {
   int n = 0, m = 0;
   DBuf<T> l_own, u_own, c_own, b_own;
   const T *l = nullptr, *u = nullptr, *c = nullptr, *b = nullptr;
-  DBuf<T> x, dx, kty, sx, skty, ax, agrad, grad, rx, rgrad, tmp_n;
+  DBuf<T> x, dx, kty, sx, ax, agrad, grad, rx, rgrad, tmp_n;
   DBuf<T> y0, y1, kx0, kx1, sy, skx, ay, akx, ry, rkx, tmp_m;
   DBuf<StepState> st_dev;
   PinnedBuf<StepState> st_host;
@@ -165,7 +153,7 @@ struct Workspace {
       if (m) launch_convert_d2f(P->b.get(), b_own.get(), m, s);
       l = l_own.get(); u = u_own.get(); c = c_own.get(); b = b_own.get();
     }
-    for (DBuf<T>* v : {&x, &dx, &kty, &sx, &skty, &ax, &agrad, &grad, &rx, &rgrad, &tmp_n}) v->alloc(N);
+    for (DBuf<T>* v : {&x, &dx, &kty, &sx, &ax, &agrad, &grad, &rx, &rgrad, &tmp_n}) v->alloc(N);
     for (DBuf<T>* v : {&y0, &y1, &kx0, &kx1, &sy, &skx, &ay, &akx, &ry, &rkx, &tmp_m}) v->alloc(M);
     rvar.alloc(N);
     rcon.alloc(M);
@@ -217,7 +205,7 @@ struct Workspace {
 
   PrimalArgs<T> primal_args(int mode) {
     return PrimalArgs<T>{P->At.view<T>(), plan_p.view(), c, l, u, x.get(), dx.get(), kty.get(), sx.get(),
-                         skty.get(), y0.get(), y1.get(), st_dev.get(), part_p.get(), part_p_split.get(), mode, direct};
+                         y0.get(), y1.get(), st_dev.get(), part_p.get(), part_p_split.get(), mode, direct};
   }
   DualArgs<T> dual_args(int mode) {
     return DualArgs<T>{P->A.view<T>(), plan_d.view(), plan_p.inst_cta_begin.get(), plan_p.inst_split_begin.get(),
@@ -285,7 +273,7 @@ struct Workspace {
 
   void spmv(const DeviceMatrix& M, const T* xin, T* yout) {
     if (M.num_items == 0) return;
-    spmv_kernel<T><<<M.num_items, kBlock, 0, P->stream>>>(M.view<T>(), xin, yout);
+    spmv_kernel<T><<<M.num_items, kBlock, 0, P->stream>>>(M.view<T>(), xin, yout, nullptr, nullptr);
     CK_LAUNCH();
     ++P->launches;
   }
@@ -390,24 +378,17 @@ bool run_phase(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopS
         st.pending_commit = 0;
       }
       const int p = st.parity;
-      // One pass per side (EvalPassN / EvalPassM): the average, or the current point
+      // One pass per side (EvalPassM, then EvalPassN): the average, or the current point
       // (src/primal_dual_hybrid_gradient_gpu.jl:635-642); its unscaled statistics
       // (src/iteration_stats_utils_gpu.jl:447-502); buffer_primal_gradient = c - K'y (:742);
       // and the restart scheme's KKT ingredients, those of the last restart point only when
-      // it moved since they were computed. One read-back for all of them.
+      // it moved since they were computed. Between them the average's K'y = A' y-bar (the
+      // reference sums the steps' K'y with the averaging weights instead; the two agree in
+      // exact arithmetic). One read-back for all of them.
       const bool use_current = st.numerical_error || st.count_primal == 0 || st.count_dual == 0;
       const double wx = st.sum_w_primal, wy = st.sum_w_dual;
       const double rwx = use_current ? 0.0 : 1.0 / wx, rwy = use_current ? 0.0 : 1.0 / wy;
       const bool with_restart = !W.restart_kkt_valid;
-      W.template reduce<kEvalNQ + kKktNQ, kEvalNMax>(
-          true,
-          EvalPassN<T>{EvalN<T>{W.ax.get(), W.agrad.get(), P->var.get(), W.rvar.get(), P->ol.get(), P->ou.get(),
-                                P->oc.get()},
-                       KktN<T>{W.l, W.u, W.c, W.x.get(), W.ax.get(), W.rx.get(), W.grad.get(), W.agrad.get(),
-                               W.rgrad.get()},
-                       W.sx.get(), W.skty.get(), W.kty.get(), W.ax.get(), W.agrad.get(), W.grad.get(), wx, wy, rwx,
-                       rwy, use_current ? 1 : 0, with_restart ? 1 : 0},
-          0);
       W.template reduce<kEvalMQ + kKktMQ, kEvalMMax>(
           false,
           EvalPassM<T>{EvalM<T>{W.ay.get(), W.akx.get(), P->con.get(), W.rcon.get(), P->ob.get(), P->neq, nullptr},
@@ -416,6 +397,16 @@ bool run_phase(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopS
                        W.sy.get(), W.skx.get(), W.ay.get(), W.akx.get(), wx, wy, rwx, rwy, use_current ? 1 : 0,
                        with_restart ? 1 : 0},
           32);
+      if (!use_current) W.spmv(P->At, W.ay.get(), W.tmp_n.get());
+      W.template reduce<kEvalNQ + kKktNQ, kEvalNMax>(
+          true,
+          EvalPassN<T>{EvalN<T>{W.ax.get(), W.agrad.get(), P->var.get(), W.rvar.get(), P->ol.get(), P->ou.get(),
+                                P->oc.get()},
+                       KktN<T>{W.l, W.u, W.c, W.x.get(), W.ax.get(), W.rx.get(), W.grad.get(), W.agrad.get(),
+                               W.rgrad.get()},
+                       W.sx.get(), W.tmp_n.get(), W.kty.get(), W.ax.get(), W.agrad.get(), W.grad.get(), wx, wy, rwx,
+                       rwy, use_current ? 1 : 0, with_restart ? 1 : 0},
+          0);
       W.fetch_reductions(32 + kEvalMQ + kKktMQ);
       const double* en = W.red_host.p;            // EvalN, then KktN at kEvalNQ
       const double* em = W.red_host.p + 32;       // EvalM, then KktM at kEvalMQ
@@ -523,7 +514,6 @@ bool run_phase(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopS
           W.restart_kkt_valid = false;  // the restart point moves below
           // reset_solution_weighted_average!
           CK(cudaMemsetAsync(W.sx.get(), 0, sizeof(T) * n, s));
-          CK(cudaMemsetAsync(W.skty.get(), 0, sizeof(T) * n, s));
           if (m) {
             CK(cudaMemsetAsync(W.sy.get(), 0, sizeof(T) * m, s));
             CK(cudaMemsetAsync(W.skx.get(), 0, sizeof(T) * m, s));
@@ -599,7 +589,7 @@ template <class T>
 void init_state(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopState& L) {
   cudaStream_t s = P->stream;
   const int n = P->n, m = P->m;
-  for (DBuf<T>* v : {&W.x, &W.kty, &W.sx, &W.skty, &W.dx, &W.ax, &W.agrad})
+  for (DBuf<T>* v : {&W.x, &W.kty, &W.sx, &W.dx, &W.ax, &W.agrad})
     CK(cudaMemsetAsync(v->get(), 0, sizeof(T) * v->n, s));
   for (DBuf<T>* v : {&W.y0, &W.y1, &W.kx0, &W.kx1, &W.sy, &W.skx, &W.ay, &W.akx})
     CK(cudaMemsetAsync(v->get(), 0, sizeof(T) * v->n, s));
@@ -694,7 +684,7 @@ void handoff_to_fp64(gpdhg_problem* P, Workspace<float>& F, Workspace<double>& D
     CK_LAUNCH();
     ++P->launches;
   };
-  conv(F.x, D.x); conv(F.dx, D.dx); conv(F.sx, D.sx); conv(F.skty, D.skty); conv(F.ax, D.ax);
+  conv(F.x, D.x); conv(F.dx, D.dx); conv(F.sx, D.sx); conv(F.ax, D.ax);
   conv(F.agrad, D.agrad); conv(F.grad, D.grad); conv(F.rx, D.rx); conv(F.rgrad, D.rgrad);
   conv(F.y0, D.y0); conv(F.y1, D.y1); conv(F.sy, D.sy); conv(F.skx, D.skx); conv(F.ay, D.ay);
   conv(F.akx, D.akx); conv(F.ry, D.ry); conv(F.rkx, D.rkx);
@@ -707,7 +697,6 @@ void handoff_to_fp64(gpdhg_problem* P, Workspace<float>& F, Workspace<double>& D
   // sums (and the K x-bar they imply) are only consistent to ~1e-7 and would feed a
   // phantom residual to the dual update after a restart to the average.
   CK(cudaMemsetAsync(D.sx.get(), 0, sizeof(double) * D.sx.n, s));
-  CK(cudaMemsetAsync(D.skty.get(), 0, sizeof(double) * D.skty.n, s));
   CK(cudaMemsetAsync(D.sy.get(), 0, sizeof(double) * D.sy.n, s));
   CK(cudaMemsetAsync(D.skx.get(), 0, sizeof(double) * D.skx.n, s));
   st.count_primal = st.count_dual = 0;

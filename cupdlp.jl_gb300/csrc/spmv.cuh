@@ -147,4 +147,22 @@ __device__ __forceinline__ void spmv_item(const CsrView<T>& M, const T* __restri
   if (owner) post(r, sum, p);
 }
 
+// y = M x over the row-block items of M. With row_inst non-NULL only the items whose first
+// row belongs to an instance with active[instance] set run (the packed matrix of a batch;
+// an item never spans two instances).
+struct NoPre {};
+template <class T>
+__global__ void __launch_bounds__(kBlock) spmv_kernel(CsrView<T> M, const T* __restrict__ x, T* y,
+                                                      const int32_t* __restrict__ row_inst,
+                                                      const uint8_t* __restrict__ active) {
+  __shared__ T stage[kStage];
+  __shared__ T stage2[sizeof(T) == 8 ? kStage : 1];
+  __shared__ T wsum[kBlock / 32];
+  if ((int)blockIdx.x >= M.num_items) return;
+  if (row_inst && !active[row_inst[M.items[blockIdx.x].row_begin]]) return;
+  auto pre = [](int) { return NoPre{}; };
+  auto post = [&](int i, T s, const NoPre&) { y[i] = s; };
+  spmv_item(M, x, blockIdx.x, stage, stage2, wsum, pre, post);
+}
+
 }  // namespace gpdhg

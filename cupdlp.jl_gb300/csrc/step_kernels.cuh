@@ -12,7 +12,8 @@
 // Here one attempt is two kernels over warp tiles (tiles.h, tile_spmv.cuh) and no host
 // round trip:
 //   primal_step_kernel: [if the previous attempt was accepted] K'y = A' y (tiles of A'),
-//       x += dx, and the x / K'y weighted sums; then the next dx, and per-CTA ||dx||^2.
+//       x += dx, and the x weighted sum; then the next dx, and per-CTA ||dx||^2. (The
+//       average's K'y is formed at evaluation time as A' y-bar, not summed here.)
 //   dual_step_kernel:   [if the previous attempt was accepted] the y / Kx weighted sums;
 //       then K dx (tiles of A), the projected dual candidate, Kx + K dx into the other half
 //       of the double-buffered y / Kx, per-CTA interaction and ||dy||^2 partials; the last
@@ -61,7 +62,6 @@ struct PrimalArgs {
   T* dx;                 // dx, or x^ in direct mode
   T* kty;
   T* sx;
-  T* skty;
   const T* y0;
   const T* y1;
   StepState* st;         // one per instance
@@ -141,7 +141,6 @@ struct PrimalIn {
   T dx;  // dx (x^ in direct mode); K'y when no commit is pending
   T x;
   T sx;
-  T sk;
   T c;
   T l;
   T u;
@@ -190,7 +189,6 @@ __global__ void __launch_bounds__(kBlock, kPrimalCtasPerSm<T>) primal_step_kerne
       e.dx = lds(a.dx + j);
       if (!direct) e.x = lds(a.x + j);
       e.sx = lds(a.sx + j);
-      e.sk = lds(a.skty + j);
     } else {
       e.x = lds(a.x + j);
       e.dx = lds(a.kty + j);
@@ -222,8 +220,7 @@ __global__ void __launch_bounds__(kBlock, kPrimalCtasPerSm<T>) primal_step_kerne
         const T xv = direct ? e.dx : e.x + e.dx;   // x += dx (:303)
         sts(a.x + j, xv);
         sts(a.kty + j, ktyv);                       // K'y = A'y (:307)
-        sts(a.sx + j, e.sx + xv * w);               // weighted sums (src/saddle_point_gpu.jl:137,182)
-        sts(a.skty + j, e.sk + ktyv * w);
+        sts(a.sx + j, e.sx + xv * w);               // weighted sum (src/saddle_point_gpu.jl:137)
         if (!commit_only) candidate(j, xv, ktyv, e, t, split);
       }
       __syncwarp();
