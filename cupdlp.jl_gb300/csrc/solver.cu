@@ -383,8 +383,9 @@ bool run_phase(gpdhg_problem* P, Workspace<T>& W, const gpdhg_params& prm, LoopS
       // (src/iteration_stats_utils_gpu.jl:447-502); buffer_primal_gradient = c - K'y (:742);
       // and the restart scheme's KKT ingredients, those of the last restart point only when
       // it moved since they were computed. Between them the average's K'y = A' y-bar (the
-      // reference sums the steps' K'y with the averaging weights instead; the two agree in
-      // exact arithmetic). One read-back for all of them.
+      // reference sums the steps' K'y with the averaging weights instead,
+      // src/saddle_point_gpu.jl:176-189; the two agree in exact arithmetic). One read-back
+      // for all of them.
       const bool use_current = st.numerical_error || st.count_primal == 0 || st.count_dual == 0;
       const double wx = st.sum_w_primal, wy = st.sum_w_dual;
       const double rwx = use_current ? 0.0 : 1.0 / wx, rwy = use_current ? 0.0 : 1.0 / wy;
