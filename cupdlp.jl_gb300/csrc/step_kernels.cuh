@@ -16,9 +16,11 @@
 //       average's K'y is formed at evaluation time as A' y-bar, not summed here.)
 //   dual_step_kernel:   [if the previous attempt was accepted] the y / Kx weighted sums;
 //       then K dx (tiles of A), the projected dual candidate, Kx + K dx into the other half
-//       of the double-buffered y / Kx, per-CTA interaction and ||dy||^2 partials; the last
-//       CTA of an instance to finish reduces that instance's partials in a fixed order and
-//       takes the accept/reject and step-size decision, flipping the buffer parity on accept.
+//       of the double-buffered y / Kx, per-CTA interaction and ||dy||^2 partials; the
+//       instance's first CTA also sums the primal kernel's ||dx||^2 partials and prepares
+//       the decision's inputs that need no dual partial; the last CTA of an instance to
+//       finish reduces that instance's dual partials in a fixed order and takes the
+//       accept/reject and step-size decision, flipping the buffer parity on accept.
 //       (A separate decision kernel measured slower: one more kernel boundary per attempt
 //       costs more than this CTA's serial tail.)
 // Every CTA belongs to one instance; each warp owns whole tiles (row sums in registers,
