@@ -155,3 +155,19 @@ def test_csc_entry_rejects_bad_input_before_any_gpu_work(lib):
     assert st == _abi.ERR_INVALID_PROBLEM and "constraint matrix" in msg
     st, msg = _csc_err(lib, p, mutate=lambda cp, rv, nz: cp.__setitem__(-1, cp[-1] + 1))
     assert st == _abi.ERR_INVALID_PROBLEM and "nnz" in msg
+
+
+def test_batch_reports_the_first_invalid_instance(lib):
+    """A batch validates its instances on host threads; the error reported is the one of the
+    lowest-numbered invalid instance, as a serial loop would report."""
+    p, _ = instances.tiny()
+    good = unscaled_desc(p)
+    nan = unscaled_desc(p)
+    nan.arrays["vals"][0] = np.nan
+    col = unscaled_desc(p)
+    col.arrays["cols"][0] = 5
+    for order, want in (((good, nan, col), "constraint matrix"), ((good, col, nan), "column index")):
+        arr = (_abi.LpDesc * 3)(*[d.desc for d in order])
+        h = C.c_void_p()
+        assert lib.gpdhg_batch_create(3, arr, C.byref(h)) == _abi.ERR_INVALID_PROBLEM
+        assert want in lib.gpdhg_last_error().decode()
