@@ -171,22 +171,23 @@ def barrier(pg):
         pg.barrier()
 
 
-def max_over_ranks(pg, v):
+def _reduce_over_ranks(pg, v, op):
     if pg is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    # NCCL reduces device tensors, gloo (the CPU fallback) host tensors
+    dev = "cuda" if pg.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(pg, v):
+    return v if pg is None else _reduce_over_ranks(pg, v, pg.ReduceOp.MAX)
 
 
 def sum_over_ranks(pg, v):
-    if pg is None:
-        return v
-    import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    pg.all_reduce(t, op=pg.ReduceOp.SUM)
-    return float(t.item())
+    return v if pg is None else _reduce_over_ranks(pg, v, pg.ReduceOp.SUM)
 
 
 PROFILE_FILES = {"transportation": "step_kernels_transportation_fp64.md", "powerlaw": "step_kernels_powerlaw_fp32.md"}
