@@ -52,7 +52,8 @@ void build_seg_items(const std::vector<int32_t>& off, std::vector<SegItem>& item
 }
 
 // Runs f(k) for k in [0, count) on host threads, instances handed out in order from a shared
-// counter; each call writes only instance k's own outputs.
+// counter; each call writes only instance k's own outputs. An exception thrown by f(k) is
+// rethrown after all threads joined: that of the lowest such k, as a serial loop would.
 template <class F>
 void for_each_instance(int count, F f) {
   const int T = std::max(1, std::min<int>(count, (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
@@ -60,14 +61,23 @@ void for_each_instance(int count, F f) {
     for (int k = 0; k < count; ++k) f(k);
     return;
   }
+  std::vector<std::exception_ptr> err(count);
   std::atomic<int> next{0};
   std::vector<std::thread> th;
   th.reserve(T);
   for (int t = 0; t < T; ++t)
     th.emplace_back([&] {
-      for (int k = next++; k < count; k = next++) f(k);
+      for (int k = next++; k < count; k = next++) {
+        try {
+          f(k);
+        } catch (...) {
+          err[k] = std::current_exception();
+        }
+      }
     });
   for (auto& x : th) x.join();
+  for (int k = 0; k < count; ++k)
+    if (err[k]) std::rethrow_exception(err[k]);
 }
 
 void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
@@ -82,18 +92,7 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
   B->neq.resize(count);
   // every descriptor validated (on host threads, one instance each); the error of the first
   // invalid instance is the one reported, as a serial loop would
-  {
-    std::vector<std::exception_ptr> err(count);
-    for_each_instance(count, [&](int k) {
-      try {
-        validate_lp_desc(&descs[k], false);
-      } catch (...) {
-        err[k] = std::current_exception();
-      }
-    });
-    for (int k = 0; k < count; ++k)
-      if (err[k]) std::rethrow_exception(err[k]);
-  }
+  for_each_instance(count, [&](int k) { validate_lp_desc(&descs[k], false); });
   long long nnz_total = 0;
   std::vector<long long> nnz_off(count + 1, 0);
   for (int k = 0; k < count; ++k) {
