@@ -195,6 +195,39 @@ gpdhg_status gpdhg_problem_create_csc(const gpdhg_lp_desc* desc, const int64_t* 
   });
 }
 
+gpdhg_status gpdhg_problem_create_two_sided(const gpdhg_two_sided_desc* desc, const int64_t* col_ptr,
+                                            const int64_t* row_val, const double* nz_val, int32_t index_base,
+                                            const gpdhg_params* unscaled_params, gpdhg_problem** out) {
+  return guarded([&] {
+    if (!out) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (!desc) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "desc is NULL");
+    if (unscaled_params && unscaled_params->l_inf_ruiz_iterations < 0)
+      throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "l_inf_ruiz_iterations must be >= 0");
+    gpdhg_problem* p = new gpdhg_problem();
+    try {
+      gpdhg::problem_init_two_sided(p, desc, col_ptr, row_val, nz_val, index_base);
+      if (unscaled_params) gpdhg::rescale_on_device(p, *unscaled_params);
+    } catch (...) {
+      delete p;
+      throw;
+    }
+    *out = p;
+  });
+}
+
+gpdhg_status gpdhg_get_standard_form(const gpdhg_problem* p, int32_t* num_variables, int32_t* num_equalities,
+                                     int32_t* num_slacks, int32_t* new_row_to_old) {
+  return guarded([&] {
+    if (!p) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "problem is NULL");
+    if (num_variables) *num_variables = p->n;
+    if (num_equalities) *num_equalities = p->neq;
+    if (num_slacks) *num_slacks = p->num_slacks;
+    if (new_row_to_old)
+      for (int32_t r = 0; r < p->m; ++r) new_row_to_old[r] = p->new_row_to_old.empty() ? r : p->new_row_to_old[r];
+  });
+}
+
 gpdhg_status gpdhg_get_rescaling(const gpdhg_problem* p, double* constraint_rescaling, double* variable_rescaling) {
   return guarded([&] {
     if (!p) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "problem is NULL");

@@ -1,5 +1,6 @@
 // problem.cu — validation and upload of one LP (replaces src/cpu_to_gpu.jl:26-81).
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <thread>
@@ -200,9 +201,11 @@ namespace {
 
 // The part of problem creation after validation: build(s) uploads one of the two CSR copies
 // and builds the other on the device; meanwhile a helper thread forms the host scalars
-// (serial sums) from the matrix values and the vectors.
+// (serial sums) from the matrix values (the first num_values of them; any others have
+// magnitude at most amax_floor) and the vectors.
 template <class Build>
-void init_with(gpdhg_problem* p, const gpdhg_lp_desc* d, const double* values, Build build) {
+void init_with(gpdhg_problem* p, const gpdhg_lp_desc* d, const double* values, int64_t num_values,
+               double amax_floor, Build build) {
   const int32_t m = d->num_constraints, n = d->num_variables;
   p->n = n;
   p->m = m;
@@ -211,10 +214,9 @@ void init_with(gpdhg_problem* p, const gpdhg_lp_desc* d, const double* values, B
   p->obj_const = d->objective_constant;
   CK(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
   cudaStream_t s = p->stream;
-  const int64_t nnz = d->nnz;
-  std::thread scalars([p, d, m, n, values, nnz] {
-    double amax = 0.0;
-    for (int64_t k = 0; k < nnz; ++k) amax = std::max(amax, std::fabs(values[k]));
+  std::thread scalars([p, d, m, n, values, num_values, amax_floor] {
+    double amax = amax_floor;
+    for (int64_t k = 0; k < num_values; ++k) amax = std::max(amax, std::fabs(values[k]));
     p->amax = amax;
     p->norm2_c_scaled = norm2(d->objective_vector, n);
     p->norm2_b_scaled = m ? norm2(d->right_hand_side, m) : 0.0;
@@ -264,43 +266,187 @@ void narrow_indices(const int64_t* src, int64_t len, int64_t base, std::vector<i
 
 void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d) {
   validate_lp_desc(d, true);
-  init_with(p, d, d->values, [&](cudaStream_t s) {
+  init_with(p, d, d->values, d->nnz, 0.0, [&](cudaStream_t s) {
     upload_csr(p->A, d->num_constraints, d->num_variables, d->row_ptr, d->col_idx, d->values, s);
     transpose_on_device(p->A, p->At, s);
   });
 }
+
+namespace {
+
+// Structure of a CSC matrix with int64 indices from index_base (Julia's SparseMatrixCSC
+// invariants): col_ptr monotone from base, nnz = col_ptr[n] - base, row indices in range,
+// finite values.
+void validate_csc(int32_t n, int32_t m, int64_t nnz_declared, const int64_t* col_ptr, const int64_t* row_val,
+                  const double* nz_val, int32_t base) {
+  if (base != 0 && base != 1) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "index_base must be 0 or 1");
+  if (!col_ptr) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "col_ptr is NULL");
+  if (col_ptr[0] != base) throw Error(GPDHG_ERR_INVALID_PROBLEM, "col_ptr[0] must be index_base");
+  if (first_bad(n, [&](int64_t j) { return col_ptr[j + 1] < col_ptr[j]; }, true) >= 0)
+    throw Error(GPDHG_ERR_INVALID_PROBLEM, "col_ptr is not monotone");
+  const int64_t nnz = col_ptr[n] - base;
+  if (nnz != nnz_declared) throw Error(GPDHG_ERR_INVALID_PROBLEM, "nnz does not match col_ptr[n] - index_base");
+  if (nnz >= (1LL << 31)) throw Error(GPDHG_ERR_INVALID_PROBLEM, "more than 2^31 - 1 nonzeros");
+  if (nnz > 0 && (!row_val || !nz_val)) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "row_val/nz_val NULL");
+  auto bad_row = [&](int64_t k) { return row_val[k] < base || row_val[k] >= (int64_t)m + base; };
+  const int64_t k = first_bad(nnz, [&](int64_t q) { return bad_row(q) || !std::isfinite(nz_val[q]); }, true);
+  if (k >= 0) {
+    if (bad_row(k)) throw Error(GPDHG_ERR_INVALID_PROBLEM, "row index out of range");
+    throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN or Inf found in constraint matrix");
+  }
+}
+
+// val[k] = -val[k] where the entry's row is flagged (the reference's `nzval[idx] *= -1` for
+// "<=" rows, src/quadratic_programming_io.jl:52-56; an exact sign flip either way).
+__global__ void negate_rows_kernel(long long nnz, const int32_t* __restrict__ row, const uint8_t* __restrict__ flip,
+                                   double* __restrict__ val) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nnz && flip[row[k]]) val[k] = -val[k];
+}
+
+}  // namespace
 
 void problem_init_csc(gpdhg_problem* p, const gpdhg_lp_desc* d, const int64_t* col_ptr, const int64_t* row_val,
                       const double* nz_val, int32_t base) {
   validate_dims(d);
   if (d->row_ptr || d->col_idx || d->values)
     throw Error(GPDHG_ERR_INVALID_ARGUMENT, "a CSC descriptor carries no row_ptr, col_idx or values");
-  if (base != 0 && base != 1) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "index_base must be 0 or 1");
-  if (!col_ptr) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "col_ptr is NULL");
   const int32_t m = d->num_constraints, n = d->num_variables;
-  if (col_ptr[0] != base) throw Error(GPDHG_ERR_INVALID_PROBLEM, "col_ptr[0] must be index_base");
-  if (first_bad(n, [&](int64_t j) { return col_ptr[j + 1] < col_ptr[j]; }, true) >= 0)
-    throw Error(GPDHG_ERR_INVALID_PROBLEM, "col_ptr is not monotone");
-  const int64_t nnz = col_ptr[n] - base;
-  if (nnz != d->nnz) throw Error(GPDHG_ERR_INVALID_PROBLEM, "nnz does not match col_ptr[n] - index_base");
-  if (nnz >= (1LL << 31)) throw Error(GPDHG_ERR_INVALID_PROBLEM, "more than 2^31 - 1 nonzeros");
-  if (nnz > 0 && (!row_val || !nz_val)) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "row_val/nz_val NULL");
-  {
-    auto bad_row = [&](int64_t k) { return row_val[k] < base || row_val[k] >= (int64_t)m + base; };
-    const int64_t k = first_bad(nnz, [&](int64_t q) { return bad_row(q) || !std::isfinite(nz_val[q]); }, true);
-    if (k >= 0) {
-      if (bad_row(k)) throw Error(GPDHG_ERR_INVALID_PROBLEM, "row index out of range");
-      throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN or Inf found in constraint matrix");
-    }
-  }
+  validate_csc(n, m, d->nnz, col_ptr, row_val, nz_val, base);
+  const int64_t nnz = d->nnz;
   validate_vectors(d, true);
-  init_with(p, d, nz_val, [&](cudaStream_t s) {
+  init_with(p, d, nz_val, nnz, 0.0, [&](cudaStream_t s) {
     // CSC(A) read as CSR(A'): its pointers become A's row pointer after the device transpose
     std::vector<int32_t> rp, ri;
     narrow_indices(col_ptr, (int64_t)n + 1, base, rp);
     narrow_indices(row_val, nnz, base, ri);
     upload_csr(p->At, n, m, rp.data(), ri.data(), nz_val, s);
     transpose_on_device(p->At, p->A, s);
+  });
+}
+
+void problem_init_two_sided(gpdhg_problem* p, const gpdhg_two_sided_desc* t, const int64_t* col_ptr,
+                            const int64_t* row_val, const double* nz_val, int32_t base) {
+  if (!t) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "descriptor is NULL");
+  const int32_t n = t->num_variables, m = t->num_constraints;
+  if (n <= 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "num_variables must be positive");
+  if (m < 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "num_constraints must be >= 0");
+  if (!t->variable_lower_bound || !t->variable_upper_bound || !t->objective_vector ||
+      (m > 0 && (!t->constraint_lower_bound || !t->constraint_upper_bound)))
+    throw Error(GPDHG_ERR_INVALID_ARGUMENT, "required array pointer is NULL");
+  validate_csc(n, m, t->nnz, col_ptr, row_val, nz_val, base);
+  const int64_t nnz = t->nnz;
+  const double* lc = t->constraint_lower_bound;
+  const double* uc = t->constraint_upper_bound;
+  for (int32_t i = 0; i < m; ++i)
+    if (std::isnan(lc[i]) || std::isnan(uc[i])) throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN found in constraint bounds");
+  // two_sided_rows_to_slacks (:85-121): rows with finite, unequal bounds get a slack column
+  // (-1 in that row) with the row's bounds, and become "= 0" rows
+  std::vector<int32_t> slack_row;
+  for (int32_t i = 0; i < m; ++i)
+    if (std::isfinite(lc[i]) && std::isfinite(uc[i]) && lc[i] != uc[i]) slack_row.push_back(i);
+  const int32_t k = (int32_t)slack_row.size();
+  if ((int64_t)n + k > INT32_MAX) throw Error(GPDHG_ERR_INVALID_PROBLEM, "too many variables after adding slacks");
+  if (nnz + k >= (1LL << 31)) throw Error(GPDHG_ERR_INVALID_PROBLEM, "more than 2^31 - 1 nonzeros");
+  std::vector<double> lo(lc, lc + m), hi(uc, uc + m);
+  for (int32_t r : slack_row) lo[r] = hi[r] = 0.0;
+  // transform_to_standard_form (:33-76): equality rows first, ">=" rows keep their sign,
+  // "<=" rows are negated; each block keeps the caller's row order
+  std::vector<uint8_t> eq(m), leq(m);
+  std::vector<int32_t> new_row_to_old;
+  new_row_to_old.reserve(m);
+  for (int32_t i = 0; i < m; ++i) {
+    eq[i] = lo[i] == hi[i];
+    const bool geq = !eq[i] && std::isfinite(lo[i]);
+    leq[i] = !eq[i] && std::isfinite(hi[i]);
+    if (!eq[i] && !geq && !leq[i])
+      throw Error(GPDHG_ERR_INVALID_PROBLEM, "Not all constraints have finite bounds on at least one side.");
+    if (eq[i]) new_row_to_old.push_back(i);
+  }
+  const int32_t neq = (int32_t)new_row_to_old.size();
+  for (int32_t i = 0; i < m; ++i)
+    if (!eq[i]) new_row_to_old.push_back(i);
+  std::vector<int32_t> old_to_new(m);
+  bool identity = true;
+  for (int32_t r = 0; r < m; ++r) {
+    old_to_new[new_row_to_old[r]] = r;
+    identity = identity && new_row_to_old[r] == r;
+  }
+  std::vector<double> rhs(m);
+  std::vector<uint8_t> flip_new(std::max(m, 1), 0);
+  for (int32_t r = 0; r < m; ++r) {
+    const int32_t i = new_row_to_old[r];
+    rhs[r] = leq[i] ? -hi[i] : lo[i];
+    flip_new[r] = leq[i];
+  }
+  const int32_t ns = n + k;
+  std::vector<double> l(t->variable_lower_bound, t->variable_lower_bound + n);
+  std::vector<double> u(t->variable_upper_bound, t->variable_upper_bound + n);
+  std::vector<double> c(t->objective_vector, t->objective_vector + n);
+  for (int32_t r : slack_row) {
+    l.push_back(lc[r]);
+    u.push_back(uc[r]);
+    c.push_back(0.0);
+  }
+  gpdhg_lp_desc d{};
+  d.num_variables = ns;
+  d.num_constraints = m;
+  d.num_equalities = neq;
+  d.nnz = nnz + k;
+  d.variable_lower_bound = l.data();
+  d.variable_upper_bound = u.data();
+  d.objective_vector = c.data();
+  d.right_hand_side = rhs.data();
+  d.objective_constant = t->objective_offset;
+  validate_vectors(&d, true);
+  p->new_row_to_old = new_row_to_old;
+  p->num_slacks = k;
+  init_with(p, &d, nz_val, nnz, k ? 1.0 : 0.0, [&](cudaStream_t s) {
+    // CSC([A S]) is CSR([A S]'), with A's row indices renumbered on the host threads that
+    // narrow them; the slack columns hold one -1 each
+    std::vector<int32_t> rp, ri;
+    narrow_indices(col_ptr, (int64_t)n + 1, base, rp);
+    narrow_indices(row_val, nnz, base, ri);
+    rp.resize((size_t)ns + 1);
+    ri.resize((size_t)(nnz + k));
+    for (int32_t j = 0; j < k; ++j) {
+      rp[(size_t)n + 1 + j] = (int32_t)(nnz + j + 1);
+      ri[(size_t)(nnz + j)] = slack_row[j];
+    }
+    if (!identity) {
+      const int T = (int)std::max<int64_t>(1, std::min<int64_t>(16, (nnz + k) / 65536));
+      std::vector<std::thread> th;
+      for (int q = 0; q < T; ++q)
+        th.emplace_back([&, q] {
+          for (int64_t e = (nnz + k) * q / T; e < (nnz + k) * (q + 1) / T; ++e) ri[(size_t)e] = old_to_new[ri[(size_t)e]];
+        });
+      for (auto& x : th) x.join();
+    }
+    DeviceMatrix& At = p->At;
+    At.nrows = ns;
+    At.ncols = m;
+    At.nnz = nnz + k;
+    At.host_rp = rp;
+    At.row_ptr.alloc((size_t)ns + 1);
+    At.col.alloc(std::max<long long>(At.nnz, 1));
+    At.val64.alloc(std::max<long long>(At.nnz, 1));
+    DBuf<uint8_t> flip((size_t)flip_new.size());
+    CK(cudaMemcpyAsync(At.row_ptr.get(), rp.data(), sizeof(int32_t) * ((size_t)ns + 1), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(flip.get(), flip_new.data(), flip_new.size(), cudaMemcpyHostToDevice, s));
+    std::vector<double> minus_one((size_t)std::max(k, 1), -1.0);
+    if (At.nnz) CK(cudaMemcpyAsync(At.col.get(), ri.data(), sizeof(int32_t) * At.nnz, cudaMemcpyHostToDevice, s));
+    if (nnz) {
+      CK(cudaMemcpyAsync(At.val64.get(), nz_val, sizeof(double) * nnz, cudaMemcpyHostToDevice, s));
+      negate_rows_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, At.col.get(), flip.get(), At.val64.get());
+      CK_LAUNCH();
+    }
+    if (k) CK(cudaMemcpyAsync(At.val64.get() + nnz, minus_one.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    // A is sorted out of A' as for any CSC; after a row renumbering, A' is rebuilt from A so
+    // that its rows list their entries in increasing row again, as row_permute_in_place
+    // leaves the columns of the CSC. The transposes synchronise the stream before returning,
+    // so the host vectors above outlive the copies that read them.
+    transpose_on_device(At, p->A, s);
+    if (!identity) transpose_on_device(p->A, At, s);
   });
 }
 

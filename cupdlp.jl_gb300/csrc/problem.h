@@ -121,6 +121,10 @@ struct gpdhg_problem {
   std::vector<double> warm_x, warm_y;   // scaled warm start (empty: zero start)
   int last_precision = -1;              // workspace holding the last current iterate
   long long launches = 0;               // kernels launched on this handle so far
+  // standard-form conversion of a two-sided problem: the caller's row behind each row, and
+  // how many slack variables follow the caller's variables (empty / 0 otherwise)
+  std::vector<int32_t> new_row_to_old;
+  int32_t num_slacks = 0;
   ~gpdhg_problem();
 };
 
@@ -135,6 +139,10 @@ void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d);
 // Julia's SparseMatrixCSC): CSC(A) is uploaded as CSR(A') and A is built on the device.
 void problem_init_csc(gpdhg_problem* p, const gpdhg_lp_desc* d, const int64_t* col_ptr, const int64_t* row_val,
                       const double* nz_val, int32_t base);
+// transform_to_standard_form (src/quadratic_programming_io.jl:33-121) while the problem is
+// built from a two-sided LP in compressed sparse columns; the matrix work runs on the device.
+void problem_init_two_sided(gpdhg_problem* p, const gpdhg_two_sided_desc* t, const int64_t* col_ptr,
+                            const int64_t* row_val, const double* nz_val, int32_t base);
 // dst[k] = (float)src[k] on stream s.
 void launch_convert_d2f(const double* src, float* dst, long long n, cudaStream_t s);
 // dst[k] = 1 / src[k] on stream s.

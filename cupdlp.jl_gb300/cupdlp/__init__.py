@@ -9,7 +9,7 @@ from .types import *  # noqa: F401,F403
 from .types import (AdaptiveStepsizeParams, ConstantStepsizeParams, ConvergenceInformation,  # noqa: F401
                     InfeasibilityInformation, IterationStats, PdhgParameters, Precision,
                     QuadraticProgrammingProblem, RestartParameters, SaddlePointOutput, ScaledQpProblem,
-                    SolveLog, TerminationCriteria, TerminationReason, construct_restart_parameters,
+                    SolveLog, TerminationCriteria, TerminationReason, TwoSidedQpProblem, construct_restart_parameters,
                     construct_termination_criteria, default_parameters, default_restart_parameters,
                     params_to_c, termination_reason_to_string, validate_termination_criteria)
 from .preprocess import (InvalidProblemError, l2_norm_rescaling, pock_chambolle_rescaling,  # noqa: F401

@@ -158,6 +158,20 @@ class LpDesc(C.Structure):
     ]
 
 
+class TwoSidedDesc(C.Structure):
+    _fields_ = [
+        ("num_variables", C.c_int32),
+        ("num_constraints", C.c_int32),
+        ("nnz", C.c_int64),
+        ("variable_lower_bound", _dp),
+        ("variable_upper_bound", _dp),
+        ("constraint_lower_bound", _dp),
+        ("constraint_upper_bound", _dp),
+        ("objective_vector", _dp),
+        ("objective_offset", C.c_double),
+    ]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [
         ("hbm_budget_bytes", C.c_double),
@@ -181,6 +195,10 @@ SIGNATURES = {
     "gpdhg_get_rescaling": (C.c_int, [C.c_void_p, _dp, _dp]),
     "gpdhg_problem_create_csc": (C.c_int, [C.POINTER(LpDesc), _lp, _lp, _dp, C.c_int32, C.POINTER(Params),
                                            C.POINTER(C.c_void_p)]),
+    "gpdhg_problem_create_two_sided": (C.c_int, [C.POINTER(TwoSidedDesc), _lp, _lp, _dp, C.c_int32,
+                                                 C.POINTER(Params), C.POINTER(C.c_void_p)]),
+    "gpdhg_get_standard_form": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                          C.POINTER(C.c_int32), _ip]),
     "gpdhg_solve": (C.c_int, [C.c_void_p, C.POINTER(Params), C.POINTER(Result), _dp, _dp]),
     "gpdhg_get_stats": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(IterationStats)]),
     "gpdhg_set_warm_start": (C.c_int, [C.c_void_p, _dp, _dp]),

@@ -14,11 +14,12 @@ import time
 from typing import List, Optional
 
 import numpy as np
+import scipy.sparse as sp
 
 from . import _abi
 from .preprocess import csr_arrays, is_linear_programming_problem, rescale_problem, validate
 from .types import (PdhgParameters, QuadraticProgrammingProblem, SaddlePointOutput, ScaledQpProblem,
-                    TerminationReason, params_to_c, stats_from_c, termination_reason_to_string)
+                    TerminationReason, TwoSidedQpProblem, params_to_c, stats_from_c, termination_reason_to_string)
 
 
 class _Desc:
@@ -113,6 +114,49 @@ class DeviceProblem:
                                                      C.byref(cp) if cp is not None else None, C.byref(h)), self.lib)
         self.handle = h
         return self
+
+    @classmethod
+    def from_two_sided(cls, qp: TwoSidedQpProblem, index_base: int = 0,
+                       unscaled_params: Optional[PdhgParameters] = None, lib=None):
+        """gpdhg_problem_create_two_sided: transform_to_standard_form
+        (src/quadratic_programming_io.jl:33-121) while the problem is built, the matrix work on
+        the GPU; with unscaled_params the standard form is then rescaled on the GPU. The
+        handle solves the standard form: see standard_form() for its size and row order."""
+        self = cls.__new__(cls)
+        self.lib = lib or _abi.load()
+        a = sp.csc_matrix(qp.constraint_matrix)
+        f64 = lambda v: np.ascontiguousarray(v, dtype=np.float64)
+        keep = dict(l=f64(qp.variable_lower_bound), u=f64(qp.variable_upper_bound),
+                    lc=f64(qp.constraint_lower_bound), uc=f64(qp.constraint_upper_bound),
+                    c=f64(qp.objective_vector), colptr=np.ascontiguousarray(a.indptr, dtype=np.int64) + index_base,
+                    rowval=np.ascontiguousarray(a.indices, dtype=np.int64) + index_base, nzval=f64(a.data))
+        d = _abi.TwoSidedDesc()
+        d.num_variables, d.num_constraints = a.shape[1], a.shape[0]
+        d.nnz = int(keep["nzval"].size)
+        d.variable_lower_bound = _abi.dptr(keep["l"])
+        d.variable_upper_bound = _abi.dptr(keep["u"])
+        d.constraint_lower_bound = _abi.dptr(keep["lc"])
+        d.constraint_upper_bound = _abi.dptr(keep["uc"])
+        d.objective_vector = _abi.dptr(keep["c"])
+        d.objective_offset = float(qp.objective_offset)
+        cp = params_to_c(unscaled_params) if unscaled_params is not None else None
+        h = C.c_void_p()
+        _abi.check(self.lib.gpdhg_problem_create_two_sided(C.byref(d), _abi.lptr(keep["colptr"]),
+                                                           _abi.lptr(keep["rowval"]), _abi.dptr(keep["nzval"]),
+                                                           int(index_base), C.byref(cp) if cp is not None else None,
+                                                           C.byref(h)), self.lib)
+        self.handle = h
+        self.m = a.shape[0]
+        self.n = self.standard_form()[0]
+        return self
+
+    def standard_form(self):
+        """(variables, equalities, slacks, new_row_to_old) of the problem the handle solves."""
+        nv, neq, ns = C.c_int32(), C.c_int32(), C.c_int32()
+        order = np.empty(self.m, dtype=np.int32)
+        _abi.check(self.lib.gpdhg_get_standard_form(self.handle, C.byref(nv), C.byref(neq), C.byref(ns),
+                                                    _abi.iptr(order)), self.lib)
+        return nv.value, neq.value, ns.value, order
 
     @classmethod
     def from_unscaled(cls, p: QuadraticProgrammingProblem, params: PdhgParameters, lib=None):

@@ -18,6 +18,9 @@ numpy.random.default_rng(seed).
   batch_lps             256 instances: m log-normal (median 2,000, clipped to [200, 50,000]),
                         n = 2m, nnz/row ~ U(5,40); 25% transportation-structured with
                         S + D = m, S = round(m/5), and m reduced until S*D <= 1,000,000.
+  two_sided_lp          a planted-optimum LP rewritten as an MPS reader returns it: '>=' rows
+                        split three ways into '>=', negated '<=' and two-sided rows (upper
+                        bound 0.5-2 above the planted A x*), then all rows shuffled.
   serving_stream        Poisson arrivals; mixture 70% small (m 200-2k), 25% medium
                         (m 10k-100k), 5% large (m 500k, nnz 10M).
 """
@@ -29,7 +32,7 @@ from typing import List, Optional
 import numpy as np
 import scipy.sparse as sp
 
-from .types import QuadraticProgrammingProblem
+from .types import QuadraticProgrammingProblem, TwoSidedQpProblem
 
 ROW_POPULARITY_EXPONENT = 0.5
 
@@ -90,6 +93,59 @@ def known_optimum_lp(seed: int = 0, m: int = 1000, n: int = 2000, neq: Optional[
     a = sp.csc_matrix((vals, (rows, cols)), shape=(m, n))
     a.sort_indices()
     return _planted(rng, a, neq, np.full(n, 10.0), f"known_optimum_m{m}_n{n}_s{seed}")
+
+
+@dataclasses.dataclass
+class SyntheticTwoSidedLp:
+    problem: TwoSidedQpProblem
+    name: str
+    optimal_objective: Optional[float] = None   # the planted optimum's, unchanged by the rewrite
+
+
+def two_sided_lp(seed: int = 5, m: int = 400, n: int = 900, neq: Optional[int] = None,
+                 density: float = 0.01) -> SyntheticTwoSidedLp:
+    """known_optimum_lp's LP as constraint_lower_bound <= A x <= constraint_upper_bound: '='
+    rows keep l = u = b; each '>=' row stays (b, +Inf), is negated into (-Inf, -b), or gets a
+    finite upper bound 0.5-2 above A x* (x* stays feasible, hence optimal); rows shuffled."""
+    base = known_optimum_lp(seed, m=m, n=n, neq=neq, density=density)
+    rng = np.random.default_rng(seed + 1000)
+    p = base.problem
+    a = sp.csr_matrix(p.constraint_matrix)
+    b = p.right_hand_side
+    lo, hi = b.copy(), b.copy()
+    ineq = np.arange(p.num_equalities, m)
+    kind = rng.integers(0, 3, ineq.size)
+    hi[ineq] = np.inf
+    neg = ineq[kind == 1]
+    lo[neg], hi[neg] = -np.inf, -b[neg]
+    two = ineq[kind == 2]
+    hi[two] = (a @ base.x_star)[two] + rng.uniform(0.5, 2.0, two.size)
+    sign = np.ones(m)
+    sign[neg] = -1.0
+    a = sp.diags(sign) @ a
+    perm = rng.permutation(m)
+    qp = TwoSidedQpProblem(p.variable_lower_bound.copy(), p.variable_upper_bound.copy(), lo[perm], hi[perm],
+                           sp.csc_matrix(a[perm]), 0.0, p.objective_vector.copy())
+    qp.constraint_matrix.sort_indices()
+    return SyntheticTwoSidedLp(qp, f"two_sided_m{m}_n{n}_s{seed}", base.optimal_objective)
+
+
+def transportation_two_sided(seed: int = 1, supplies: int = 500, demands: int = 2000) -> SyntheticTwoSidedLp:
+    """transportation_lp as its MPS file states it: demand rows '=' and supply rows '<='
+    (sum_j x_ij <= s_i), before the reader's standard-form conversion."""
+    t = transportation_lp(seed, supplies, demands).problem
+    D = t.num_equalities
+    a = sp.csr_matrix(t.constraint_matrix)
+    sign = np.ones(t.num_constraints)
+    sign[D:] = -1.0
+    lo = t.right_hand_side.copy()
+    hi = t.right_hand_side.copy()
+    lo[D:] = -np.inf
+    hi[D:] = -t.right_hand_side[D:]
+    qp = TwoSidedQpProblem(t.variable_lower_bound.copy(), t.variable_upper_bound.copy(), lo, hi,
+                           sp.csc_matrix(sp.diags(sign) @ a), 0.0, t.objective_vector.copy())
+    qp.constraint_matrix.sort_indices()
+    return SyntheticTwoSidedLp(qp, f"transportation_two_sided_{supplies}x{demands}_s{seed}")
 
 
 def transportation_lp(seed: int = 1, supplies: int = 500, demands: int = 2000) -> SyntheticLp:

@@ -115,6 +115,27 @@ class QuadraticProgrammingProblem:
 
 
 @dataclasses.dataclass
+class TwoSidedQpProblem:
+    """TwoSidedQpProblem (src/quadratic_programming_io.jl:5-22) of an LP: l <= x <= u and
+    constraint_lower_bound <= A x <= constraint_upper_bound (the MPS reader's form)."""
+    variable_lower_bound: np.ndarray
+    variable_upper_bound: np.ndarray
+    constraint_lower_bound: np.ndarray
+    constraint_upper_bound: np.ndarray
+    constraint_matrix: sp.spmatrix
+    objective_offset: float
+    objective_vector: np.ndarray
+
+    @property
+    def num_variables(self) -> int:
+        return int(self.constraint_matrix.shape[1])
+
+    @property
+    def num_constraints(self) -> int:
+        return int(self.constraint_matrix.shape[0])
+
+
+@dataclasses.dataclass
 class ScaledQpProblem:
     original_qp: QuadraticProgrammingProblem
     scaled_qp: QuadraticProgrammingProblem

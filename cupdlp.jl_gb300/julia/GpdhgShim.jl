@@ -230,4 +230,71 @@ function solve(params, scaled_problem; precision::Integer = 0)
     end
 end
 
+struct GpdhgTwoSidedDesc
+    num_variables::Int32
+    num_constraints::Int32
+    nnz::Int64
+    variable_lower_bound::Ptr{Float64}
+    variable_upper_bound::Ptr{Float64}
+    constraint_lower_bound::Ptr{Float64}
+    constraint_upper_bound::Ptr{Float64}
+    objective_vector::Ptr{Float64}
+    objective_offset::Float64
+end
+
+"""
+    solve_two_sided(params, qp::TwoSidedQpProblem; precision=0)
+
+The MPS path (`qps_reader_to_standard_form`, src/quadratic_programming_io.jl:139-186)
+without the host conversion: `transform_to_standard_form` (:33-121) and `rescale_problem`
+run on the GPU inside gpdhg_problem_create_two_sided, then the loop runs as in `solve`.
+Returns (primal, dual, termination_reason, iteration_count, new_row_to_old,
+num_equalities): the UNSCALED average of the standard form (slack variables after the
+original ones; rows in the standard form's order, i.e. row r is the caller's row
+new_row_to_old[r], 1-based, negated when that row was a "<=" row), which is what the
+reference's MPS path returns.
+"""
+function solve_two_sided(params, qp; precision::Integer = 0)
+    A = qp.constraint_matrix
+    m, n = size(A)
+    colptr = convert(Vector{Int64}, A.colptr)
+    rowval = convert(Vector{Int64}, A.rowval)
+    nzval = convert(Vector{Float64}, A.nzval)
+    arrays = (colptr, rowval, nzval, qp.variable_lower_bound, qp.variable_upper_bound,
+              qp.constraint_lower_bound, qp.constraint_upper_bound, qp.objective_vector)
+    result = Ref{GpdhgResult}()
+    GC.@preserve arrays begin
+        desc = Ref(GpdhgTwoSidedDesc(Int32(n), Int32(m), Int64(length(nzval)), pointer(qp.variable_lower_bound),
+                                     pointer(qp.variable_upper_bound), pointer(qp.constraint_lower_bound),
+                                     pointer(qp.constraint_upper_bound), pointer(qp.objective_vector),
+                                     qp.objective_offset))
+        cp = Ref(c_params(params, precision))
+        handle = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:gpdhg_problem_create_two_sided, libgpdhg), Cint,
+                    (Ref{GpdhgTwoSidedDesc}, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Int32, Ref{GpdhgParams},
+                     Ref{Ptr{Cvoid}}),
+                    desc, colptr, rowval, nzval, Int32(1), cp, handle))
+        try
+            nv, neq, ns = Ref{Int32}(0), Ref{Int32}(0), Ref{Int32}(0)
+            order = zeros(Int32, m)
+            check(ccall((:gpdhg_get_standard_form, libgpdhg), Cint,
+                        (Ptr{Cvoid}, Ref{Int32}, Ref{Int32}, Ref{Int32}, Ptr{Int32}), handle[], nv, neq, ns, order))
+            primal = zeros(nv[])
+            dual = zeros(m)
+            check(ccall((:gpdhg_solve, libgpdhg), Cint,
+                        (Ptr{Cvoid}, Ref{GpdhgParams}, Ref{GpdhgResult}, Ptr{Float64}, Ptr{Float64}),
+                        handle[], cp, result, primal, dual))
+            con = zeros(m)
+            var = zeros(nv[])
+            check(ccall((:gpdhg_get_rescaling, libgpdhg), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}),
+                        handle[], con, var))
+            # unscaled_saddle_point_output (src/saddle_point_gpu.jl:40-61)
+            return primal ./ var, dual ./ con, result[].termination_reason, result[].iteration_count,
+                   order .+ 1, Int(neq[])
+        finally
+            ccall((:gpdhg_problem_destroy, libgpdhg), Cint, (Ptr{Cvoid},), handle[])
+        end
+    end
+end
+
 end # module

@@ -290,6 +290,49 @@ gpdhg_status gpdhg_problem_create_csc(const gpdhg_lp_desc* desc, const int64_t* 
                                       gpdhg_problem** out);
 
 /*
+ * TwoSidedQpProblem (src/quadratic_programming_io.jl:5-22) with a zero objective matrix:
+ * l <= x <= u and constraint_lower_bound <= A x <= constraint_upper_bound, as an MPS
+ * reader returns it. The matrix is passed separately in compressed sparse columns.
+ */
+typedef struct gpdhg_two_sided_desc {
+  int32_t num_variables;               /* n */
+  int32_t num_constraints;             /* m */
+  int64_t nnz;
+  const double* variable_lower_bound;  /* n */
+  const double* variable_upper_bound;  /* n */
+  const double* constraint_lower_bound; /* m, may hold -Inf */
+  const double* constraint_upper_bound; /* m, may hold +Inf */
+  const double* objective_vector;      /* n */
+  double objective_offset;
+} gpdhg_two_sided_desc;
+
+/*
+ * transform_to_standard_form (src/quadratic_programming_io.jl:33-76, with
+ * two_sided_rows_to_slacks :85-121 and row_permute_in_place, src/preprocess.jl:586-611)
+ * done while the problem is built: each row with two finite, unequal bounds becomes
+ * A x - s = 0 with a new variable s in [lower, upper] (appended after the n variables, in
+ * row order); rows with only a finite upper bound are negated into ">=" rows; equality rows
+ * move to the front, each block keeping its row order. The matrix (CSC, index base 0 or 1,
+ * as for gpdhg_problem_create_csc) is uploaded once: the sign flips, the row renumbering,
+ * the slack entries and both CSR copies are made on the device. With `unscaled_params` the
+ * standard-form problem is then rescaled on the device as by gpdhg_problem_create_unscaled;
+ * with NULL it is solved unscaled. A row with neither bound finite fails with
+ * GPDHG_ERR_INVALID_PROBLEM, as the reference's error() does.
+ */
+gpdhg_status gpdhg_problem_create_two_sided(const gpdhg_two_sided_desc* desc, const int64_t* col_ptr,
+                                            const int64_t* row_val, const double* nz_val, int32_t index_base,
+                                            const gpdhg_params* unscaled_params, gpdhg_problem** out);
+/*
+ * The standard form a handle solves: its variable count (n plus one slack per two-sided
+ * row), equality count, slack count and, in new_row_to_old (m entries, 0-based), the row
+ * of the caller's problem behind each standard-form row (the reference's new_row_to_old).
+ * For a handle not made by gpdhg_problem_create_two_sided: n, num_equalities, 0 and the
+ * identity. Any output pointer may be NULL.
+ */
+gpdhg_status gpdhg_get_standard_form(const gpdhg_problem* p, int32_t* num_variables, int32_t* num_equalities,
+                                     int32_t* num_slacks, int32_t* new_row_to_old);
+
+/*
  * Runs the restarted PDHG loop of optimize() (src/primal_dual_hybrid_gradient_gpu.jl:
  * 494-797) on the handle's problem from a zero starting point (or the warm start set
  * with gpdhg_set_warm_start). On return `primal_out` (n) and `dual_out` (m) hold the
