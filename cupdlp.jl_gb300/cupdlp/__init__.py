@@ -12,8 +12,9 @@ from .types import (AdaptiveStepsizeParams, ConstantStepsizeParams, ConvergenceI
                     SolveLog, TerminationCriteria, TerminationReason, TwoSidedQpProblem, construct_restart_parameters,
                     construct_termination_criteria, default_parameters, default_restart_parameters,
                     params_to_c, termination_reason_to_string, validate_termination_criteria)
-from .preprocess import (InvalidProblemError, l2_norm_rescaling, pock_chambolle_rescaling,  # noqa: F401
-                         rescale_problem, ruiz_rescaling, scale_problem, unscale_problem, validate)
+from .preprocess import (InfeasibleProblemError, InvalidProblemError, PresolveInfo,  # noqa: F401
+                         l2_norm_rescaling, pock_chambolle_rescaling, presolve, rescale_problem, ruiz_rescaling,
+                         scale_problem, undo_presolve, unscale_problem, validate)
 from .solver import (DeviceBatch, DeviceProblem, Server, optimize, optimize_batch, scaled_desc,  # noqa: F401
                      unscaled_desc)
 from . import _abi  # noqa: F401

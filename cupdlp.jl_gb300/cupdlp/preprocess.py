@@ -7,6 +7,7 @@
   pock_chambolle_rescaling  src/preprocess.jl:494-525
   scale_problem             src/preprocess.jl:541-561
   rescale_problem           src/preprocess.jl:619-675
+  presolve / undo_presolve  src/preprocess.jl:105-326 (defined by the reference, never called)
 
 Matrices are scipy CSC, as the reference's SparseMatrixCSC. Row-wise reductions go
 through a fixed CSC->CSR permutation of the nonzeros (the pattern never changes while
@@ -16,6 +17,7 @@ Only the LP case (objective_matrix == 0) is supported, as on the solve path.
 from __future__ import annotations
 
 import copy
+import dataclasses
 import math
 
 import numpy as np
@@ -230,3 +232,132 @@ def csr_arrays(a, pattern: _Pattern | None = None):
         raise ValueError("nnz must fit int32")
     return (np.ascontiguousarray(c.indptr, dtype=np.int32), np.ascontiguousarray(c.indices, dtype=np.int32),
             np.ascontiguousarray(c.data, dtype=np.float64))
+
+
+# ---- presolve (src/preprocess.jl:105-326) --------------------------------------------------
+# The reference defines presolve / undo_presolve but optimize() never calls them; they are
+# mirrored here so a caller that wants them finds them with the same behaviour (indices are
+# 0-based here, 1-based in Julia).
+
+class InfeasibleProblemError(ValueError):
+    """remove_empty_rows' `error("The problem is infeasible.")` (src/preprocess.jl:118-123)."""
+
+
+@dataclasses.dataclass
+class PresolveInfo:
+    """src/preprocess.jl:210-217."""
+    original_primal_size: int
+    original_dual_size: int
+    empty_rows: np.ndarray
+    empty_columns: np.ndarray
+    variable_lower_bound: np.ndarray
+    variable_upper_bound: np.ndarray
+
+
+def remove_empty_rows(p: QuadraticProgrammingProblem) -> np.ndarray:
+    """Drops rows without nonzeros; an empty '=' row needs b = 0 and an empty '>=' row b <= 0,
+    else the problem is infeasible (src/preprocess.jl:112-133)."""
+    _ensure_csc(p)
+    a = p.constraint_matrix
+    seen = np.zeros(a.shape[0], dtype=bool)
+    seen[a.indices] = True
+    empty = np.flatnonzero(~seen)
+    b = p.right_hand_side
+    for row in empty:
+        if row >= p.num_equalities and b[row] > 0.0:
+            raise InfeasibleProblemError("The problem is infeasible.")
+        if row < p.num_equalities and b[row] != 0.0:
+            raise InfeasibleProblemError("The problem is infeasible.")
+    if empty.size:
+        p.constraint_matrix = sp.csc_matrix(a[seen, :])
+        p.right_hand_side = b[seen]
+        p.num_equalities -= int((empty < p.num_equalities).sum())
+    return empty
+
+
+def remove_empty_columns(p: QuadraticProgrammingProblem) -> np.ndarray:
+    """Drops variables without nonzeros, fixing each at its best bound in the objective
+    constant: the lower bound when c_j >= 0, else the upper (src/preprocess.jl:143-171; an
+    infinite best bound makes the constant infinite, and 0 * Inf NaN, as there)."""
+    assert is_linear_programming_problem(p)
+    _ensure_csc(p)
+    a = p.constraint_matrix
+    is_empty = np.diff(a.indptr) == 0
+    empty = np.flatnonzero(is_empty)
+    if empty.size == 0:
+        return empty
+    const = float(p.objective_constant)
+    for col in empty:   # one addition at a time, in column order, as the reference's loop
+        coef = p.objective_vector[col]
+        const += (p.variable_lower_bound[col] if coef >= 0 else p.variable_upper_bound[col]) * coef
+    p.objective_constant = const
+    keep = ~is_empty
+    p.constraint_matrix = sp.csc_matrix(a[:, keep])
+    p.objective_vector = p.objective_vector[keep]
+    p.variable_lower_bound = p.variable_lower_bound[keep]
+    p.variable_upper_bound = p.variable_upper_bound[keep]
+    n = int(keep.sum())
+    p.objective_matrix = sp.csc_matrix((n, n), dtype=np.float64)
+    return empty
+
+
+def transform_bounds_into_linear_constraints(p: QuadraticProgrammingProblem) -> None:
+    """Appends a '>=' row x_j >= l_j per finite lower bound, then -x_j >= -u_j per finite upper
+    bound, and frees the variables (src/preprocess.jl:176-207)."""
+    _ensure_csc(p)
+    lo = np.flatnonzero(np.isfinite(p.variable_lower_bound))
+    hi = np.flatnonzero(np.isfinite(p.variable_upper_bound))
+    k = lo.size + hi.size
+    n = p.constraint_matrix.shape[1]
+    block = sp.csc_matrix((np.concatenate([np.ones(lo.size), -np.ones(hi.size)]),
+                           (np.arange(k), np.concatenate([lo, hi]))), shape=(k, n))
+    p.constraint_matrix = sp.csc_matrix(sp.vstack([p.constraint_matrix, block], format="csc"))
+    p.right_hand_side = np.concatenate([p.right_hand_side, p.variable_lower_bound[lo], -p.variable_upper_bound[hi]])
+    p.variable_lower_bound = np.full(n, -np.inf)
+    p.variable_upper_bound = np.full(n, np.inf)
+
+
+def check_for_singleton_constraints(p: QuadraticProgrammingProblem) -> int:
+    """Counts (and reports) rows with exactly one nonzero (src/preprocess.jl:262-276)."""
+    _ensure_csc(p)
+    per_row = np.bincount(p.constraint_matrix.indices, minlength=p.constraint_matrix.shape[0])
+    single = int((per_row == 1).sum())
+    if single > 0:
+        print(f"{single} constraints involving exactly a single variable")
+    return single
+
+
+def presolve(p: QuadraticProgrammingProblem, verbosity: int = 1, transform_bounds: bool = False) -> PresolveInfo:
+    """Modifies p in place; the returned record undoes it (src/preprocess.jl:223-258)."""
+    saved_lo = p.variable_lower_bound.copy()
+    saved_hi = p.variable_upper_bound.copy()
+    original_dual_size, original_primal_size = p.constraint_matrix.shape
+    empty_rows = remove_empty_rows(p)
+    if is_linear_programming_problem(p):
+        empty_columns = remove_empty_columns(p)
+    else:
+        empty_columns = np.zeros(0, dtype=np.int64)
+    if verbosity >= 1:
+        check_for_singleton_constraints(p)
+    if transform_bounds:
+        transform_bounds_into_linear_constraints(p)
+    return PresolveInfo(original_primal_size, original_dual_size, empty_rows, empty_columns, saved_lo, saved_hi)
+
+
+def recover_original_solution(solution: np.ndarray, empty_indices: np.ndarray, original_size: int) -> np.ndarray:
+    """Zeros at the removed indices, the solution's leading entries elsewhere in order
+    (src/preprocess.jl:290-299)."""
+    keep = np.ones(original_size, dtype=bool)
+    keep[np.asarray(empty_indices, dtype=np.int64)] = False
+    out = np.zeros(original_size)
+    out[keep] = np.asarray(solution)[: int(keep.sum())]
+    return out
+
+
+def undo_presolve(info: PresolveInfo, primal_solution: np.ndarray, dual_solution: np.ndarray):
+    """(primal, dual) of the problem before presolve; the primal is projected onto the saved
+    bounds (src/preprocess.jl:301-326)."""
+    primal = recover_original_solution(primal_solution, info.empty_columns, info.original_primal_size)
+    primal = np.minimum(np.maximum(primal, info.variable_lower_bound), info.variable_upper_bound)
+    dual = recover_original_solution(dual_solution, info.empty_rows, info.original_dual_size)
+    return primal, dual
