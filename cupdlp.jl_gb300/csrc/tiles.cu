@@ -88,19 +88,22 @@ void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector
     const size_t t0 = tiles.size();
     list_tiles(M.host_rp.data(), bounds[k], bounds[k + 1], k, aux.empty() ? 0 : aux[k], TileTraits<T>::kNnz,
                TileTraits<T>::kEMax, tiles, splits, carries);
-    // CTAs: 8 / W group tiles of one width W together; other consecutive tiles of this
-    // instance in groups of tpc: 8 while the instance has fewer tiles than one per warp of
+    // warp-streamed rows first, in row order, then the other tiles in row order: CTAs then
+    // hold one kind of work (a power-law A' scatters thousands of such rows among short ones)
+    std::stable_partition(tiles.begin() + t0, tiles.end(), [](const Tile& t) { return t.e_log2 == kWarpLong; });
+    // CTAs: 8 / W group tiles of one width W together; warp-streamed rows, and the other
+    // tiles, in groups of tpc: 8 while the instance has fewer tiles than one per warp of
     // every resident CTA slot (152 SMs x ctas_per_sm), then as many as make the instance's
     // CTAs one wave, up to kTilesPerCtaMax
     const long long nt = (long long)(tiles.size() - t0);
     const long long slots = 152LL * ctas_per_sm;
     const long long tpc = std::min<long long>(kTilesPerCtaMax, std::max<long long>(kTilesPerCtaMin, (nt + slots - 1) / slots));
     long long open = 0;   // tiles in the CTA being filled
-    int open_code = 0;    // its tiles' kind: 0 normal, else the group code
+    int open_code = 0;    // its tiles' kind: 0 normal, kWarpLong, else the group code
     for (size_t q = t0; q < tiles.size(); ++q) {
       const int e = tiles[q].e_log2;
-      const int code = e <= group_code(1) ? e : 0;
-      const long long cap = code ? (8 >> group_log2(code)) : tpc;
+      const int code = e < 0 ? e : 0;
+      const long long cap = code <= group_code(1) ? (8 >> group_log2(code)) : tpc;
       if (open == 0 || code != open_code || open == cap) {
         cta_begin.push_back((int32_t)q);
         cta_inst.push_back(k);
