@@ -1,5 +1,6 @@
 // problem.cu — validation and upload of one LP (replaces src/cpu_to_gpu.jl:26-81).
 #include <algorithm>
+#include <array>
 #include <climits>
 #include <cmath>
 #include <cstring>
@@ -96,33 +97,50 @@ double norm_inf(const double* v, size_t n) {
 
 namespace {
 
-// The smallest k in [0, len) with bad(k), or -1: contiguous chunks checked on host threads,
-// so the answer (and hence the error reported) is the serial scan's.
+// Host threads for a scan of len entries with `checks` tests each: one per 256k tests, at most
+// 16 (a thread's start-up costs tens of microseconds, 256k tests a few hundred).
+int scan_threads(int64_t len, int checks, bool threads) {
+  if (!threads) return 1;
+  const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
+  return (int)std::min<int64_t>(std::min<int64_t>(hw, 16), std::max<int64_t>(1, len * checks / 262144));
+}
+
+// For each of the K predicates, the smallest q in [0, len) with bad(q, k), or -1: one pass of
+// contiguous chunks on host threads, so each answer is the serial scan's.
+template <int K, class Bad>
+std::array<int64_t, K> first_bad_each(int64_t len, Bad bad, bool threads) {
+  const int T = scan_threads(len, K, threads);
+  std::vector<std::array<int64_t, K>> first(T);
+  auto scan = [&](int t) {
+    std::array<int64_t, K>& f = first[t];
+    f.fill(-1);
+    int open = K;
+    for (int64_t q = len * t / T, e = len * (t + 1) / T; q < e && open; ++q)
+      for (int k = 0; k < K; ++k)
+        if (f[k] < 0 && bad(q, k)) {
+          f[k] = q;
+          --open;
+        }
+  };
+  if (T <= 1) {
+    scan(0);
+  } else {
+    std::vector<std::thread> th;
+    th.reserve(T);
+    for (int t = 0; t < T; ++t) th.emplace_back(scan, t);
+    for (auto& x : th) x.join();
+  }
+  std::array<int64_t, K> out;
+  out.fill(-1);
+  for (int k = 0; k < K; ++k)
+    for (int t = 0; t < T && out[k] < 0; ++t) out[k] = first[t][k];
+  return out;
+}
+
+// The smallest k in [0, len) with bad(k), or -1.
 template <class Bad>
 int64_t first_bad(int64_t len, Bad bad, bool threads) {
-  const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
-  const int T = threads ? (int)std::min<int64_t>(std::min<int64_t>(hw, 32), std::max<int64_t>(1, len / 65536)) : 1;
-  if (T <= 1) {
-    for (int64_t k = 0; k < len; ++k)
-      if (bad(k)) return k;
-    return -1;
-  }
-  std::vector<int64_t> first(T, -1);
-  std::vector<std::thread> th;
-  th.reserve(T);
-  for (int t = 0; t < T; ++t)
-    th.emplace_back([&, t] {
-      const int64_t b = len * t / T, e = len * (t + 1) / T;
-      for (int64_t k = b; k < e; ++k)
-        if (bad(k)) {
-          first[t] = k;
-          return;
-        }
-    });
-  for (auto& x : th) x.join();
-  for (int t = 0; t < T; ++t)
-    if (first[t] >= 0) return first[t];
-  return -1;
+  return first_bad_each<1>(len, [&](int64_t q, int) { return bad(q); }, threads)[0];
 }
 
 }  // namespace
@@ -143,33 +161,46 @@ void validate_dims(const gpdhg_lp_desc* d) {
 
 void validate_vectors(const gpdhg_lp_desc* d, bool threads) {
   const int32_t m = d->num_constraints, n = d->num_variables;
-  auto check_bounds = [&](const double* l, const double* u) {
-    const int64_t j = first_bad(n, [&](int64_t q) {
-      return l[q] == INFINITY || u[q] == -INFINITY || std::isnan(l[q]) || std::isnan(u[q]);
-    }, threads);
-    if (j < 0) return;
-    if (l[j] == INFINITY) throw Error(GPDHG_ERR_INVALID_PROBLEM, "variable_lower_bound contains +Inf");
-    if (u[j] == -INFINITY) throw Error(GPDHG_ERR_INVALID_PROBLEM, "variable_upper_bound contains -Inf");
+  const double *l = d->variable_lower_bound, *u = d->variable_upper_bound, *c = d->objective_vector;
+  const double *ol = d->original_variable_lower_bound, *ou = d->original_variable_upper_bound;
+  const double *oc = d->original_objective_vector, *var = d->variable_rescaling;
+  const double *b = d->right_hand_side, *ob = d->original_right_hand_side, *con = d->constraint_rescaling;
+  const bool obounds = ol && ou;
+  auto bad_bounds = [](const double* lo, const double* hi, int64_t q) {
+    return lo[q] == INFINITY || hi[q] == -INFINITY || std::isnan(lo[q]) || std::isnan(hi[q]);
+  };
+  auto not_pos = [](const double* v, int64_t q) { return !(v[q] > 0.0) || !std::isfinite(v[q]); };
+  // every check of each side in one pass; failures are reported in the serial order below
+  const std::array<int64_t, 5> fn = first_bad_each<5>(n, [&](int64_t q, int k) {
+    switch (k) {
+      case 0: return bad_bounds(l, u, q);
+      case 1: return !std::isfinite(c[q]);
+      case 2: return obounds && bad_bounds(ol, ou, q);
+      case 3: return oc && !std::isfinite(oc[q]);
+      default: return var && not_pos(var, q);
+    }
+  }, threads);
+  const std::array<int64_t, 3> fm = first_bad_each<3>(m, [&](int64_t q, int k) {
+    switch (k) {
+      case 0: return !std::isfinite(b[q]);
+      case 1: return ob && !std::isfinite(ob[q]);
+      default: return con && not_pos(con, q);
+    }
+  }, threads);
+  auto bounds_error = [](const double* lo, const double* hi, int64_t j) {
+    if (lo[j] == INFINITY) throw Error(GPDHG_ERR_INVALID_PROBLEM, "variable_lower_bound contains +Inf");
+    if (hi[j] == -INFINITY) throw Error(GPDHG_ERR_INVALID_PROBLEM, "variable_upper_bound contains -Inf");
     throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN found in variable bounds");
   };
-  auto check_finite = [&](const double* v, int32_t len, const char* what) {
-    if (first_bad(len, [&](int64_t q) { return !std::isfinite(v[q]); }, threads) >= 0)
-      throw Error(GPDHG_ERR_INVALID_PROBLEM, std::string("NaN or Inf found in ") + what);
-  };
-  check_bounds(d->variable_lower_bound, d->variable_upper_bound);
-  check_finite(d->objective_vector, n, "objective vector");
-  if (m) check_finite(d->right_hand_side, m, "right hand side");
+  if (fn[0] >= 0) bounds_error(l, u, fn[0]);
+  if (fn[1] >= 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN or Inf found in objective vector");
+  if (fm[0] >= 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN or Inf found in right hand side");
   if (!std::isfinite(d->objective_constant)) throw Error(GPDHG_ERR_INVALID_PROBLEM, "objective constant not finite");
-  if (d->original_variable_lower_bound && d->original_variable_upper_bound)
-    check_bounds(d->original_variable_lower_bound, d->original_variable_upper_bound);
-  if (d->original_objective_vector) check_finite(d->original_objective_vector, n, "original objective vector");
-  if (d->original_right_hand_side && m) check_finite(d->original_right_hand_side, m, "original right hand side");
-  auto check_pos = [&](const double* v, int32_t len, const char* what) {
-    if (first_bad(len, [&](int64_t q) { return !(v[q] > 0.0) || !std::isfinite(v[q]); }, threads) >= 0)
-      throw Error(GPDHG_ERR_INVALID_PROBLEM, std::string(what) + " must be positive and finite");
-  };
-  if (d->constraint_rescaling && m) check_pos(d->constraint_rescaling, m, "constraint_rescaling");
-  if (d->variable_rescaling) check_pos(d->variable_rescaling, n, "variable_rescaling");
+  if (fn[2] >= 0) bounds_error(ol, ou, fn[2]);
+  if (fn[3] >= 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN or Inf found in original objective vector");
+  if (fm[1] >= 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "NaN or Inf found in original right hand side");
+  if (fm[2] >= 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "constraint_rescaling must be positive and finite");
+  if (fn[4] >= 0) throw Error(GPDHG_ERR_INVALID_PROBLEM, "variable_rescaling must be positive and finite");
 }
 
 }  // namespace
@@ -214,19 +245,36 @@ void init_with(gpdhg_problem* p, const gpdhg_lp_desc* d, const double* values, i
   p->obj_const = d->objective_constant;
   CK(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
   cudaStream_t s = p->stream;
-  std::thread scalars([p, d, m, n, values, num_values, amax_floor] {
-    double amax = amax_floor;
-    for (int64_t k = 0; k < num_values; ++k) amax = std::max(amax, std::fabs(values[k]));
-    p->amax = amax;
-    p->norm2_c_scaled = norm2(d->objective_vector, n);
-    p->norm2_b_scaled = m ? norm2(d->right_hand_side, m) : 0.0;
-    const double* oc = d->original_objective_vector ? d->original_objective_vector : d->objective_vector;
-    const double* ob = d->original_right_hand_side ? d->original_right_hand_side : d->right_hand_side;
+  // the scalars: each serial sum on a thread of its own (same order, same bits as one loop);
+  // the maximum |a_ij|, exact in any order, in chunks
+  const double* c = d->objective_vector;
+  const double* oc = d->original_objective_vector ? d->original_objective_vector : c;
+  const double* bv = d->right_hand_side;
+  const double* ob = d->original_right_hand_side ? d->original_right_hand_side : bv;
+  const int ta = (int)std::max<int64_t>(1, std::min<int64_t>(8, num_values >> 20));
+  std::vector<double> amax_part(ta, amax_floor);
+  std::vector<std::thread> scalars;
+  for (int t = 0; t < ta; ++t)
+    scalars.emplace_back([&amax_part, values, num_values, ta, t] {
+      double a = amax_part[t];
+      for (int64_t k = num_values * t / ta; k < num_values * (t + 1) / ta; ++k) a = std::max(a, std::fabs(values[k]));
+      amax_part[t] = a;
+    });
+  scalars.emplace_back([p, c, n] { p->norm2_c_scaled = norm2(c, n); });
+  scalars.emplace_back([p, c, oc, n] {
     p->linf_c = norm_inf(oc, n);
-    p->l2_c = norm2(oc, n);
+    if (oc != c) p->l2_c = norm2(oc, n);
+  });
+  scalars.emplace_back([p, bv, ob, m] {
+    p->norm2_b_scaled = m ? norm2(bv, m) : 0.0;
     p->linf_b = m ? norm_inf(ob, m) : 0.0;
     p->l2_b = m ? norm2(ob, m) : 0.0;
   });
+  auto join_scalars = [&] {
+    for (auto& x : scalars) x.join();
+    p->amax = *std::max_element(amax_part.begin(), amax_part.end());
+    if (oc == c) p->l2_c = p->norm2_c_scaled;
+  };
   try {
     build(s);
     std::vector<double> ones((size_t)std::max(m, n), 1.0);
@@ -243,10 +291,10 @@ void init_with(gpdhg_problem* p, const gpdhg_lp_desc* d, const double* values, i
     set_row_items(p->A, s);
     set_row_items(p->At, s);
   } catch (...) {
-    scalars.join();
+    join_scalars();
     throw;
   }
-  scalars.join();
+  join_scalars();
   CK(cudaStreamSynchronize(s));
 }
 

@@ -18,6 +18,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <exception>
 #include <thread>
 #include <limits>
 #include <random>
@@ -153,16 +154,35 @@ struct Workspace {
       if (m) launch_convert_d2f(P->b.get(), b_own.get(), m, s);
       l = l_own.get(); u = u_own.get(); c = c_own.get(); b = b_own.get();
     }
-    for (DBuf<T>* v : {&x, &dx, &kty, &sx, &ax, &agrad, &grad, &rx, &rgrad, &tmp_n}) v->alloc(N);
-    for (DBuf<T>* v : {&y0, &y1, &kx0, &kx1, &sy, &skx, &ay, &akx, &ry, &rkx, &tmp_m}) v->alloc(M);
-    rvar.alloc(N);
-    rcon.alloc(M);
-    launch_reciprocal(P->var.get(), rvar.get(), n, s);
-    launch_reciprocal(P->con.get(), rcon.get(), m, s);
-    st_dev.alloc(1);
-    CK(cudaMemsetAsync(st_dev.get(), 0, sizeof(StepState), s));
-    build_tile_plan(plan_p, P->At, {0, n}, {}, kPrimalCtasPerSm<T>, s);
-    build_tile_plan(plan_d, P->A, {0, m}, {P->neq}, kDualCtasPerSm, s);
+    // the primal plan (a host pass over the n rows of A') is built on a helper thread while
+    // this one allocates the iterate vectors and builds the dual plan
+    std::exception_ptr plan_err;
+    int device = 0;
+    CK(cudaGetDevice(&device));
+    std::thread plan_thread([&] {
+      try {
+        CK(cudaSetDevice(device));   // a new host thread starts on device 0
+        build_tile_plan(plan_p, P->At, {0, n}, {}, kPrimalCtasPerSm<T>, s);
+      } catch (...) {
+        plan_err = std::current_exception();
+      }
+    });
+    try {
+      for (DBuf<T>* v : {&x, &dx, &kty, &sx, &ax, &agrad, &grad, &rx, &rgrad, &tmp_n}) v->alloc(N);
+      for (DBuf<T>* v : {&y0, &y1, &kx0, &kx1, &sy, &skx, &ay, &akx, &ry, &rkx, &tmp_m}) v->alloc(M);
+      rvar.alloc(N);
+      rcon.alloc(M);
+      launch_reciprocal(P->var.get(), rvar.get(), n, s);
+      launch_reciprocal(P->con.get(), rcon.get(), m, s);
+      st_dev.alloc(1);
+      CK(cudaMemsetAsync(st_dev.get(), 0, sizeof(StepState), s));
+      build_tile_plan(plan_d, P->A, {0, m}, {P->neq}, kDualCtasPerSm, s);
+    } catch (...) {
+      plan_thread.join();
+      throw;
+    }
+    plan_thread.join();
+    if (plan_err) std::rethrow_exception(plan_err);
     part_p.alloc(plan_p.num_ctas);
     part_d.alloc(2 * (size_t)plan_d.num_ctas);
     part_p_split.alloc(std::max(plan_p.num_splits, 1));
