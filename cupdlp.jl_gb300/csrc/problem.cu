@@ -4,6 +4,7 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <exception>
 #include <thread>
 
 #include "problem.h"
@@ -80,6 +81,21 @@ void upload_vec(DBuf<double>& d, const double* h, size_t n, cudaStream_t s) {
 
 void upload_vec_or_fill(DBuf<double>& d, const double* h, const double* fallback, size_t n, cudaStream_t s) {
   upload_vec(d, h ? h : fallback, n, s);
+}
+
+__global__ void fill_ones_kernel(double* __restrict__ v, long long n) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) v[k] = 1.0;
+}
+
+// d = h (n entries), or all ones when h is NULL (filled on the device)
+void upload_vec_or_ones(DBuf<double>& d, const double* h, size_t n, cudaStream_t s) {
+  if (h) return upload_vec(d, h, n, s);
+  d.alloc(std::max<size_t>(n, 1));
+  if (n) {
+    fill_ones_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.get(), (long long)n);
+    CK_LAUNCH();
+  }
 }
 
 double norm2(const double* v, size_t n) {
@@ -277,19 +293,37 @@ void init_with(gpdhg_problem* p, const gpdhg_lp_desc* d, const double* values, i
   };
   try {
     build(s);
-    std::vector<double> ones((size_t)std::max(m, n), 1.0);
-    upload_vec(p->l, d->variable_lower_bound, n, s);
-    upload_vec(p->u, d->variable_upper_bound, n, s);
-    upload_vec(p->c, d->objective_vector, n, s);
-    upload_vec(p->b, d->right_hand_side, m, s);
-    upload_vec_or_fill(p->ol, d->original_variable_lower_bound, d->variable_lower_bound, n, s);
-    upload_vec_or_fill(p->ou, d->original_variable_upper_bound, d->variable_upper_bound, n, s);
-    upload_vec_or_fill(p->oc, d->original_objective_vector, d->objective_vector, n, s);
-    upload_vec_or_fill(p->ob, d->original_right_hand_side, d->right_hand_side, m, s);
-    upload_vec_or_fill(p->con, d->constraint_rescaling, ones.data(), m, s);
-    upload_vec_or_fill(p->var, d->variable_rescaling, ones.data(), n, s);
-    set_row_items(p->A, s);
-    set_row_items(p->At, s);
+    // the row-block schedules (a host pass over the rows of A and A') on a helper thread
+    // while this one uploads the vectors
+    std::exception_ptr items_err;
+    int device = 0;
+    CK(cudaGetDevice(&device));
+    std::thread items([&] {
+      try {
+        CK(cudaSetDevice(device));   // a new host thread starts on device 0
+        set_row_items(p->A, s);
+        set_row_items(p->At, s);
+      } catch (...) {
+        items_err = std::current_exception();
+      }
+    });
+    try {
+      upload_vec(p->l, d->variable_lower_bound, n, s);
+      upload_vec(p->u, d->variable_upper_bound, n, s);
+      upload_vec(p->c, d->objective_vector, n, s);
+      upload_vec(p->b, d->right_hand_side, m, s);
+      upload_vec_or_fill(p->ol, d->original_variable_lower_bound, d->variable_lower_bound, n, s);
+      upload_vec_or_fill(p->ou, d->original_variable_upper_bound, d->variable_upper_bound, n, s);
+      upload_vec_or_fill(p->oc, d->original_objective_vector, d->objective_vector, n, s);
+      upload_vec_or_fill(p->ob, d->original_right_hand_side, d->right_hand_side, m, s);
+      upload_vec_or_ones(p->con, d->constraint_rescaling, m, s);
+      upload_vec_or_ones(p->var, d->variable_rescaling, n, s);
+    } catch (...) {
+      items.join();
+      throw;
+    }
+    items.join();
+    if (items_err) std::rethrow_exception(items_err);
   } catch (...) {
     join_scalars();
     throw;
