@@ -171,3 +171,33 @@ def test_batch_reports_the_first_invalid_instance(lib):
         h = C.c_void_p()
         assert lib.gpdhg_batch_create(3, arr, C.byref(h)) == _abi.ERR_INVALID_PROBLEM
         assert want in lib.gpdhg_last_error().decode()
+
+
+def test_validation_reports_the_serial_scans_first_failure(lib):
+    """Every vector check of a side runs in one threaded pass (n = 600k: several threads); the
+    error reported is still the one a serial scan of the checks, in validate's order, meets."""
+    from cupdlp.solver import _Desc
+    n, m = 600_000, 3
+    rp = np.array([0, 1, 2, 3], dtype=np.int32)
+    cols = np.array([0, n // 2, n - 1], dtype=np.int32)
+    vals = np.ones(3)
+
+    def err(**bad):
+        v = dict(l=np.zeros(n), u=np.full(n, 10.0), c=np.ones(n), b=np.ones(m), ol=np.zeros(n), ou=np.full(n, 10.0),
+                 oc=np.ones(n), ob=np.ones(m), con=np.ones(m), var=np.ones(n))
+        for key, (idx, value) in bad.items():
+            v[key][idx] = value
+        d = _Desc(n, m, 1, rp, cols, vals, v["l"], v["u"], v["c"], v["b"], 0.0, v["ol"], v["ou"], v["oc"], v["ob"],
+                  v["con"], v["var"])
+        st, msg = _create_err(lib, d)
+        assert st == _abi.ERR_INVALID_PROBLEM
+        return msg
+
+    assert "objective vector" in err(c=(500_000, np.nan), var=(10, 0.0)) and "original" not in err(c=(5, np.inf))
+    assert "upper_bound contains -Inf" in err(u=(400_000, -np.inf), ol=(5, np.inf))
+    assert "NaN found in variable bounds" in err(l=(100_000, np.nan), u=(200_000, -np.inf))
+    assert "upper_bound contains -Inf" in err(l=(300_000, np.inf), u=(200_000, -np.inf))
+    assert "right hand side" in err(b=(2, np.nan), oc=(7, np.nan))
+    assert "original objective vector" in err(oc=(599_999, np.inf), ob=(0, np.nan), var=(1, -1.0))
+    assert "constraint_rescaling" in err(con=(1, 0.0), var=(0, np.nan))
+    assert "variable_rescaling" in err(var=(300_000, 0.0))
