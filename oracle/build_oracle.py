@@ -14,7 +14,7 @@ LIB = os.path.join(OUT_DIR, "libpdhg_oracle.so")
 # The same oracle with another summation order (64-element reduction chunks, rows of
 # every product summed last-to-first). The reference loop is chaotic in floating point,
 # so the distance between the two oracles measures how far two correct implementations
-# that only round differently drift apart; GPU parity is judged against that envelope.
+# that only round differently drift apart; GPU parity is checked against that envelope.
 LIB_PERTURBED = os.path.join(OUT_DIR, "libpdhg_oracle_perturbed.so")
 SRC = os.path.join(HERE, "pdhg_oracle.cpp")
 
