@@ -131,16 +131,18 @@ def test_ctypes_struct_sizes_match_header(tmp_path):
     import subprocess, os
     src = tmp_path / "sz.c"
     inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
-    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "gpdhg.h"\nint main(){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n",'
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "gpdhg.h"\nint main(){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n",'
                    'sizeof(gpdhg_params), sizeof(gpdhg_convergence_information), sizeof(gpdhg_infeasibility_information),'
                    'sizeof(gpdhg_iteration_stats), sizeof(gpdhg_result), sizeof(gpdhg_lp_desc), sizeof(gpdhg_server_config),'
-                   'offsetof(gpdhg_params, precision), offsetof(gpdhg_result, last_iteration_stats));return 0;}\n')
+                   'offsetof(gpdhg_params, precision), offsetof(gpdhg_result, last_iteration_stats),'
+                   'sizeof(gpdhg_two_sided_desc), offsetof(gpdhg_two_sided_desc, objective_offset));return 0;}\n')
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I", inc, str(src), "-o", str(exe)], check=True)
     got = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()))
     want = [C.sizeof(_abi.Params), C.sizeof(_abi.ConvergenceInformation), C.sizeof(_abi.InfeasibilityInformation),
             C.sizeof(_abi.IterationStats), C.sizeof(_abi.Result), C.sizeof(_abi.LpDesc), C.sizeof(_abi.ServerConfig),
-            _abi.Params.precision.offset, _abi.Result.last_iteration_stats.offset]
+            _abi.Params.precision.offset, _abi.Result.last_iteration_stats.offset,
+            C.sizeof(_abi.TwoSidedDesc), _abi.TwoSidedDesc.objective_offset.offset]
     assert got == want
 
 
