@@ -133,3 +133,21 @@ def test_two_sided_entry_rejects_bad_input_before_any_gpu_work(lib):
     h = C.c_void_p()
     assert lib.gpdhg_problem_create_two_sided(None, None, None, None, 0, None, C.byref(h)) == _abi.ERR_INVALID_ARGUMENT
     assert lib.gpdhg_get_standard_form(None, None, None, None, None) == _abi.ERR_INVALID_ARGUMENT
+
+
+def test_oracle_pdhg_on_the_standard_form_reaches_the_planted_optimum(oracle_mod):
+    """The oracle's restatement of optimize() on the oracle's standard form of a two-sided LP
+    (slacks, negated and reordered rows) terminates optimal at the planted objective."""
+    t = synthetic.two_sided_lp(6, m=150, n=400, density=0.03)
+    q = t.problem
+    sf = standard_form.transform_to_standard_form(q.variable_lower_bound, q.variable_upper_bound,
+                                                  q.constraint_lower_bound, q.constraint_upper_bound,
+                                                  q.constraint_matrix, q.objective_vector, q.objective_offset)
+    n = sf["A"].shape[1]
+    p = cupdlp.QuadraticProgrammingProblem(sf["l"], sf["u"], sp.csc_matrix((n, n)), sf["c"], sf["offset"],
+                                           sp.csc_matrix(sf["A"]), sf["b"], sf["num_equalities"])
+    params = cupdlp.default_parameters(tolerance=1e-8, iteration_limit=100_000, time_sec_limit=120.0)
+    res, x, y, _ = oracle_mod.optimize(p, params)
+    assert res.termination_reason == cupdlp.TerminationReason.TERMINATION_REASON_OPTIMAL
+    po = res.last_iteration_stats.convergence_information.primal_objective
+    assert abs(po - t.optimal_objective) <= 1e-6 * max(1.0, abs(t.optimal_objective))
