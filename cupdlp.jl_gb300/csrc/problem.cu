@@ -484,8 +484,8 @@ void problem_init_two_sided(gpdhg_problem* p, const gpdhg_two_sided_desc* t, con
   p->new_row_to_old = new_row_to_old;
   p->num_slacks = k;
   init_with(p, &d, nz_val, nnz, k ? 1.0 : 0.0, [&](cudaStream_t s) {
-    // CSC([A S]) is CSR([A S]'), with A's row indices renumbered on the host threads that
-    // narrow them; the slack columns hold one -1 each
+    // CSC([A S]) is CSR([A S]'): the narrowed row indices, renumbered on host threads when
+    // the rows move; the slack columns hold one -1 each
     std::vector<int32_t> rp, ri;
     narrow_indices(col_ptr, (int64_t)n + 1, base, rp);
     narrow_indices(row_val, nnz, base, ri);
