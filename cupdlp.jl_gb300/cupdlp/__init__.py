@@ -18,5 +18,6 @@ from .preprocess import (InfeasibleProblemError, InvalidProblemError, PresolveIn
 from .solver import (DeviceBatch, DeviceProblem, Server, optimize, optimize_batch, scaled_desc,  # noqa: F401
                      unscaled_desc)
 from . import _abi  # noqa: F401
+from . import layout  # noqa: F401
 
 __all__ = [n for n in dir() if not n.startswith("_")]
