@@ -15,7 +15,8 @@ under the reference's own criteria, with the scaled problem already resident in 
   roofline    the dominant step kernel's algorithmic bytes / its CUDA-event time, measured
               live right after the timed steps on the same number of solves launched kernel
               by kernel with an event between every two (params.profile_kernels; events
-              cannot split the kernels of a CUDA graph).
+              cannot split the kernels of a CUDA graph). traffic and
+              fp64_pipe_active_pct_ncu come from the committed ncu capture (profiles/).
   cpu_baseline  the oracle (the CPU FP64 restatement of the reference loop) on the host
               cores over a bounded sample of the same workload.
 
@@ -194,25 +195,43 @@ def sum_over_ranks(pg, v):
 PROFILE_FILES = {"transportation": "step_kernels_transportation_fp64.md", "powerlaw": "step_kernels_powerlaw_fp32.md"}
 
 
-def profile_traffic(workload_name, kernel):
-    """DRAM bytes per launch (read + write) of `kernel` in the committed ncu capture of this
-    workload (profiles/), averaged over the captured launches; None if there is none."""
+def _profile_rows(workload_name, kernel):
+    """The table rows of `kernel` in the committed ncu capture of this workload (profiles/)."""
     fn = PROFILE_FILES.get(workload_name)
     if not fn:
-        return None
+        return []
     try:
         text = open(os.path.join(REPO, "profiles", fn)).read()
     except OSError:
-        return None
-    vals = []
+        return []
+    rows = []
     for line in text.splitlines():
         cells = [c.strip() for c in line.strip().strip("|").split("|")]
-        if len(cells) > 3 and cells[0].startswith(kernel + "<"):
-            try:
-                vals.append((float(cells[2]) + float(cells[3])) * 1e6)
-            except ValueError:
-                pass
+        if len(cells) > 7 and cells[0].startswith(kernel + "<"):
+            rows.append(cells)
+    return rows
+
+
+def _profile_mean(rows, f):
+    vals = []
+    for cells in rows:
+        try:
+            vals.append(f(cells))
+        except ValueError:
+            pass
     return sum(vals) / len(vals) if vals else None
+
+
+def profile_traffic(workload_name, kernel):
+    """DRAM bytes per launch (read + write) of `kernel` in the committed ncu capture of this
+    workload, averaged over the captured launches; None if there is none."""
+    return _profile_mean(_profile_rows(workload_name, kernel), lambda c: (float(c[2]) + float(c[3])) * 1e6)
+
+
+def profile_fp64_pipe(workload_name, kernel):
+    """FP64 pipe activity (% of peak) of `kernel` in the same capture: the unit that binds the
+    FP64 kernels, which the HBM fraction alone does not show."""
+    return _profile_mean(_profile_rows(workload_name, kernel), lambda c: float(c[7]))
 
 
 def cpu_baseline(lp_problem, params, iters_cap, threads=None):
@@ -553,6 +572,7 @@ def run_ours(args):
                 "share_of_step_time": {"primal_step_kernel": tp / max(tp + td, 1e-30),
                                        "dual_step_kernel": td / max(tp + td, 1e-30)},
                 "bytes_per_launch": {"primal_with_commit": bm["primal_commit"], "dual": bm["dual"]},
+                "fp64_pipe_active_pct_ncu": profile_fp64_pipe(args.workload, dom),
                 "step_pair_GBps": ((bytes_p + bytes_d) / (tp + td) / 1e9) if tp + td > 0 else None}
 
     # e2e through the C ABI with host buffers (create -> solve -> copy back), every step
