@@ -2,19 +2,24 @@
 // computed without allocating any memory.
 //
 // Who needs it: callers that may not allocate on the GPU at the moment they want a
-// solution checked — code that runs while a stream is being captured into a CUDA graph
-// (where cudaMalloc would break the capture), code inside a host that owns all device memory
-// through its own pool (a Julia CUDA.jl or PyTorch caching allocator that must not be
-// bypassed), or a serving path with a fixed memory budget. They pass device pointers to the
-// problem vectors, the candidate and its two products, and get back the reference's
-// ConvergenceInformation.
+// solution checked — code inside a host that owns all device memory through its own pool
+// (a Julia CUDA.jl or PyTorch caching allocator that must not be bypassed), a serving path
+// with a fixed memory budget, or a process whose device memory is exhausted by design. They
+// pass device pointers to the problem vectors, the candidate and its two products, and get
+// back the reference's ConvergenceInformation.
+//
+// The call is synchronous: it ends by copying the statistics to the host and waiting for its
+// stream. It therefore cannot run on a stream that is being captured into a CUDA graph; such a
+// call is refused with GPDHG_ERR_NOT_SUPPORTED before any other CUDA call, which leaves the
+// caller's capture intact.
 //
 // Scratch: one file-scope device array (kScratchDoubles doubles, 608.3 KiB), which every GPU
-// that loads the library holds until the process exits. Its device address is looked up once
-// per device (cudaGetSymbolAddress with that device current) on the first call made on that
-// device; that first call should therefore come before any stream capture begins. Every call
-// reuses the same array: each call overwrites all partials it reads, so nothing needs
-// clearing, and calls that overlap on the GPU (two streams, or two host threads) race on it.
+// that loads the library holds until the process exits. Its device address is looked up with
+// cudaGetSymbolAddress, with the device current, on the first call in each CUDA context (once
+// per device, again only if that device's context was destroyed and re-created, since the
+// module and its symbol are reloaded then). Every call reuses the same array: each call
+// overwrites all partials it reads, so nothing needs clearing, and calls that overlap on the
+// GPU (two streams, or two host threads) race on it.
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -119,21 +124,50 @@ __global__ void __launch_bounds__(kBlock) noalloc_finalize_kernel(const double* 
   }
 }
 
-std::mutex g_addr_mutex;
-double* g_addr[256] = {};
+using CtxGetIdFn = int (*)(void* ctx, unsigned long long* id);   // cuCtxGetId
 
-// Device address of the scratch array for the current device (looked up once per device).
+// Id of the current CUDA context through the driver entry point (cudart is linked statically,
+// libcuda is not); 0 when there is none yet.
+unsigned long long current_context_id() {
+  static CtxGetIdFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      f = nullptr;
+    }
+    return reinterpret_cast<CtxGetIdFn>(f);
+  }();
+  if (!fn) throw Error(GPDHG_ERR_CUDA, "cuCtxGetId is not available from the driver");
+  unsigned long long id = 0;
+  return fn(nullptr, &id) == 0 ? id : 0ULL;
+}
+
+struct ScratchAddress {
+  unsigned long long context = 0;
+  double* ptr = nullptr;
+};
+std::mutex g_addr_mutex;
+ScratchAddress g_addr[256];
+
+// Device address of the scratch array in the current device's current context: looked up
+// once per context, so a device whose context was reset gets the reloaded module's address.
 double* scratch_address() {
   int dev = 0;
   CK(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 256) throw Error(GPDHG_ERR_CUDA, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_addr_mutex);
-  if (!g_addr[dev]) {
+  ScratchAddress& a = g_addr[dev];
+  const unsigned long long ctx = current_context_id();
+  if (!a.ptr || ctx == 0 || ctx != a.context) {
     void* p = nullptr;
-    CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_addr[dev] = static_cast<double*>(p);
+    CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));   // makes the device's primary context current
+    a.ptr = static_cast<double*>(p);
+    a.context = current_context_id();
+    if (a.context == 0) throw Error(GPDHG_ERR_CUDA, "no current CUDA context after the symbol lookup");
   }
-  return g_addr[dev];
+  return a.ptr;
 }
 
 }  // namespace
@@ -153,6 +187,15 @@ void convergence_noalloc(int32_t n, int32_t m, int32_t neq, double obj_const, co
     throw Error(GPDHG_ERR_INVALID_ARGUMENT,
                 "gpdhg_convergence_noalloc handles at most 16,777,216 variables and constraints");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // A capturing stream cannot take the synchronous read-back at the end; refuse before any
+  // other CUDA call so that the caller's capture is left valid.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  const cudaError_t ce = cudaStreamIsCapturing(s, &cap);
+  if (ce != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    if (ce != cudaSuccess) cudaGetLastError();
+    throw Error(GPDHG_ERR_NOT_SUPPORTED,
+                "gpdhg_convergence_noalloc is synchronous and cannot run on a stream that is being captured");
+  }
   double* base = scratch_address();
   double* part_n = base;
   double* part_m = base + (size_t)kQn * kNoallocMaxItems;

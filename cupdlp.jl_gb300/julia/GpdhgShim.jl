@@ -7,7 +7,7 @@
 # PDHG loop, the copy of the average back to the host) are replaced by `GpdhgShim.solve`.
 # Struct layouts mirror include/gpdhg.h field for field (all isbits, C alignment).
 #
-# Usage inside cuPDLP (see INTEGRATION.md):
+# Usage inside cuPDLP:
 #     include("GpdhgShim.jl")
 #     function optimize(params::PdhgParameters, original_problem::QuadraticProgrammingProblem)
 #         validate(original_problem)

@@ -381,15 +381,17 @@ gpdhg_status gpdhg_batch_destroy(gpdhg_batch* b);
  *
  * The reference's termination statistics (ConvergenceInformation of
  * compute_convergence_information) of a candidate (x, y) of an unscaled LP, for callers that
- * may not allocate GPU memory when they want a solution checked: code recording a CUDA graph,
- * or a host whose own memory pool owns the device. Every pointer except `out` is a DEVICE
- * pointer the caller owns: bounds and objective (n), right-hand side (m), x (n), y (m),
- * primal_product = A x (m), dual_product = A'y (n). `stream` is a cudaStream_t or NULL.
- * The library allocates nothing: its scratch is one fixed device array of 608.3 KiB that
- * every GPU loading the library holds until the process exits, so n and m are limited to
- * 16,777,216 each (GPDHG_ERR_INVALID_ARGUMENT beyond). The first call on a device looks the
- * array's address up (make it before any stream capture); calls that overlap on the GPU share
- * the array and race.
+ * may not allocate GPU memory when they want a solution checked: a host whose own memory pool
+ * owns the device (a caching allocator that must not be bypassed), or a serving path with a
+ * fixed memory budget. Every pointer except `out` is a DEVICE pointer the caller owns: bounds
+ * and objective (n), right-hand side (m), x (n), y (m), primal_product = A x (m),
+ * dual_product = A'y (n). `stream` is a cudaStream_t or NULL. The call is synchronous (it
+ * copies the statistics back and waits for `stream`), so a stream that is being captured into
+ * a CUDA graph is refused with GPDHG_ERR_NOT_SUPPORTED before any other CUDA call, leaving the
+ * capture valid. The library allocates nothing: its scratch is one fixed device array of
+ * 608.3 KiB that every GPU loading the library holds until the process exits, so n and m are
+ * limited to 16,777,216 each (GPDHG_ERR_INVALID_ARGUMENT beyond). The first call in each CUDA
+ * context looks the array's address up; calls that overlap on the GPU share the array and race.
  * ------------------------------------------------------------------------------- */
 gpdhg_status gpdhg_convergence_noalloc(int32_t num_variables, int32_t num_constraints, int32_t num_equalities,
                                        double objective_constant, const double* variable_lower_bound,
