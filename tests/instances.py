@@ -47,3 +47,32 @@ def empty_rows_and_columns(seed=8):
     # a zero row (equality, rhs 0) and a zero column with a bounded variable
     A = sp.csc_matrix(np.array([[1.0, 2.0, 0.0, 0.0], [0.0, 0.0, 0.0, 0.0], [1.0, -1.0, 0.0, 1.0]]))
     return lp(A, [2.0, 0.0, 0.5], [1.0, 1.0, -1.0, 0.5], [0, 0, 0, 0], [10, 10, 3, 10], 2)
+
+
+# Row lengths that reach every work shape of the step kernels' tile plans, in A (dual kernel)
+# and in A' (primal kernel): warp-streamed rows (FP64 tiles hold 128 nonzeros, FP32 tiles 256;
+# up to 512), group tiles of 2, 4 and 8 warps (513-1,024, 1,025-2,048, 2,049-16,384) and
+# split rows cut into 16,384-nonzero pieces (20,000: two pieces, 40,000: three).
+LONG_ROW_LENGTHS = (150, 300, 600, 1500, 4000, 20000, 40000)
+
+
+def long_rows_lp(seed=31, m=45000, n=45000, per_column=2, lengths=LONG_ROW_LENGTHS):
+    """A planted-optimum LP (bounds [0, 10]) whose short rows and columns (about
+    `per_column` nonzeros per column) surround a few rows of A and a few columns of A (rows of
+    A') of the given lengths, spread over equality and inequality rows; values N(0,1)."""
+    from cupdlp import synthetic
+    rng = np.random.default_rng(seed)
+    rows = [rng.integers(0, m, per_column * n)]
+    cols = [np.repeat(np.arange(n), per_column)]
+    long_r = rng.choice(m, size=len(lengths), replace=False)
+    long_c = rng.choice(n, size=len(lengths), replace=False)
+    for r, c, k in zip(long_r, long_c, lengths):
+        rows.append(np.full(k, r))
+        cols.append(rng.choice(n, size=k, replace=False))
+        rows.append(rng.choice(m, size=k, replace=False))
+        cols.append(np.full(k, c))
+    rows, cols = np.concatenate(rows), np.concatenate(cols)
+    a = sp.csc_matrix((rng.standard_normal(rows.size), (rows, cols)), shape=(m, n))
+    a.sum_duplicates()
+    a.sort_indices()
+    return synthetic._planted(rng, a, int(round(0.6 * m)), np.full(n, 10.0), f"long_rows_m{m}_n{n}_s{seed}")
