@@ -11,7 +11,11 @@ So the pins are:
 Each instance is re-generated from (generator, seed, sizes); a checksum of the
 generated data guards against a different numpy random stream.
 
-Run:  python tests/golden/make_golden.py
+The power-law section pins reduced instances of the large power-law generator: its planted
+optimum against HiGHS, and how many iterations the oracle needs (the family converges slowly
+under PDHG: most instances with m >= 1,000 do not reach 1e-4 within 300,000 iterations).
+
+Run:  python tests/golden/make_golden.py [--power-law-only]
 """
 import hashlib
 import json
@@ -41,6 +45,16 @@ INSTANCES = [
 ]
 
 
+# Reduced power-law LPs (synthetic.power_law_lp with smaller m, n, nnz). "converge": the oracle
+# reaches 1e-8 on them; "study": HiGHS-pinned only, with the oracle's state after a fixed budget.
+POWER_LAW = [
+    {"gen": "power_law_lp", "seed": 6, "kw": {"m": 300, "n": 600, "target_nnz": 3000}, "kind": "converge"},
+    {"gen": "power_law_lp", "seed": 3, "kw": {"m": 300, "n": 600, "target_nnz": 3000}, "kind": "converge"},
+    {"gen": "power_law_lp", "seed": 7, "kw": {"m": 2000, "n": 4000, "target_nnz": 40000}, "kind": "study",
+     "budget": 20000},
+]
+
+
 def make(spec):
     return getattr(synthetic, spec["gen"])(spec["seed"], **spec["kw"])
 
@@ -54,7 +68,7 @@ def checksum(p):
     return h.hexdigest()[:16]
 
 
-def highs_objective(p):
+def highs_objective(p, presolve=True):
     a = sp.csr_matrix(p.constraint_matrix)
     neq = p.num_equalities
     bounds = list(zip(np.where(np.isfinite(p.variable_lower_bound), p.variable_lower_bound, None),
@@ -62,13 +76,49 @@ def highs_objective(p):
     res = so.linprog(p.objective_vector, A_ub=-a[neq:] if a.shape[0] > neq else None,
                      b_ub=-p.right_hand_side[neq:] if a.shape[0] > neq else None,
                      A_eq=a[:neq] if neq else None, b_eq=p.right_hand_side[:neq] if neq else None,
-                     bounds=bounds, method="highs")
+                     bounds=bounds, method="highs", options={"presolve": presolve})
     assert res.status == 0, res.message
     return float(res.fun) + p.objective_constant
 
 
+def power_law_entry(spec):
+    lp = make(spec)
+    p = lp.problem
+    entry = dict(spec)
+    entry["checksum"] = checksum(p)
+    entry["m"], entry["n"], entry["nnz"] = p.num_constraints, p.num_variables, int(p.constraint_matrix.nnz)
+    entry["planted_objective"] = lp.optimal_objective
+    # HiGHS' presolve declares one of these (coefficients spread over four decades) infeasible;
+    # its simplex without presolve reaches the planted optimum
+    entry["highs_objective"] = highs_objective(p, presolve=False)
+    if spec["kind"] == "converge":
+        for tol, key in ((1e-4, "oracle_1e4"), (1e-8, "oracle_1e8")):
+            res, x, y, st = oracle.optimize(p, cupdlp.default_parameters(tolerance=tol, iteration_limit=400000))
+            ci = res.last_iteration_stats.convergence_information
+            entry[key] = {"termination_reason": res.termination_reason, "iteration_count": res.iteration_count,
+                          "primal_objective": ci.primal_objective, "dual_objective": ci.dual_objective}
+    else:
+        res, x, y, st = oracle.optimize(p, cupdlp.default_parameters(tolerance=1e-4,
+                                                                     iteration_limit=spec["budget"]))
+        ci = res.last_iteration_stats.convergence_information
+        entry["oracle_budget"] = {"termination_reason": res.termination_reason,
+                                  "iteration_count": res.iteration_count,
+                                  "primal_objective": ci.primal_objective, "dual_objective": ci.dual_objective,
+                                  "relative_optimality_gap": ci.relative_optimality_gap,
+                                  "relative_l2_primal_residual": ci.relative_l2_primal_residual}
+    print(entry["gen"], entry["seed"], entry["highs_objective"], entry.get("oracle_1e8", entry.get("oracle_budget")))
+    return entry
+
+
 def main():
     oracle.set_threads(8)
+    path = os.path.join(HERE, "golden.json")
+    if "--power-law-only" in sys.argv:
+        out = json.load(open(path))
+        out["power_law"] = [power_law_entry(spec) for spec in POWER_LAW]
+        with open(path, "w") as f:
+            json.dump(out, f, indent=1)
+        return
     out = {"instances": []}
     for spec in INSTANCES:
         lp = make(spec)
@@ -97,7 +147,8 @@ def main():
                                  "kkt_passes": res.cumulative_kkt_matrix_passes}
         out["instances"].append(entry)
         print(entry["gen"], entry["seed"], entry["highs_objective"], entry["oracle_1e8"])
-    with open(os.path.join(HERE, "golden.json"), "w") as f:
+    out["power_law"] = [power_law_entry(spec) for spec in POWER_LAW]
+    with open(path, "w") as f:
         json.dump(out, f, indent=1)
 
 

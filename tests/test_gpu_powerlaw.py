@@ -1,0 +1,101 @@
+"""The power-law LP family on the GPU (synthetic.power_law_lp: Zipf(1.5) column degrees,
+skewed row lengths, values N(0,1) x 10^U(-2,2), boxes [0, U(1,100)]).
+
+The full-size instance (m = 1M, n = 2M, 21M nonzeros) does not reach 1e-4 within a benchmark's
+iteration budget, and neither does the oracle on reduced instances with m >= 1,000 (the
+committed golden entries). So correctness is shown on reduced instances that converge, pinned
+by HiGHS and the oracle, in FP64, FP32 and FP32 with the FP64 hand-off; at full size the
+checks are size-independent: the statistics the solver reports for its returned iterate equal
+an independent numpy evaluation of that iterate (compute_convergence_information,
+src/iteration_stats_utils_gpu.jl:251-309)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import cupdlp
+from cupdlp import synthetic
+
+from golden.make_golden import make
+from kkt import convergence_information, meets_tolerance
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))
+CONVERGE = [e for e in GOLDEN["power_law"] if e["kind"] == "converge"]
+STUDY = [e for e in GOLDEN["power_law"] if e["kind"] == "study"]
+OPT = cupdlp.TerminationReason.TERMINATION_REASON_OPTIMAL
+LIMIT = cupdlp.TerminationReason.TERMINATION_REASON_ITERATION_LIMIT
+
+
+def _params(**kw):
+    kw.setdefault("time_sec_limit", 120.0)
+    kw.setdefault("iteration_limit", 400000)
+    return cupdlp.default_parameters(**kw)
+
+
+@pytest.mark.parametrize("precision", [cupdlp.Precision.FP64, cupdlp.Precision.FP32_REFINE])
+@pytest.mark.parametrize("entry", CONVERGE, ids=lambda e: f"seed{e['seed']}")
+def test_reduced_power_law_reaches_1e8(entry, precision):
+    p = make(entry).problem
+    out = cupdlp.optimize(_params(tolerance=1e-8, precision=precision), p)
+    assert out.termination_reason == OPT
+    if precision == cupdlp.Precision.FP32_REFINE:
+        assert out.result.fp64_handoff_iteration > 0
+    ci = out.iteration_stats[-1].convergence_information[0]
+    for ref in (entry["highs_objective"], entry["oracle_1e8"]["primal_objective"]):
+        assert ci.primal_objective == pytest.approx(ref, rel=1e-6)
+        assert ci.dual_objective == pytest.approx(ref, rel=1e-6)
+    ok, k = meets_tolerance(p, out.primal_solution, out.dual_solution, 1e-8, slack=1.01)
+    assert ok, k
+    print(f"seed {entry['seed']} {precision.name}: {out.iteration_count} iterations "
+          f"(oracle {entry['oracle_1e8']['iteration_count']}), objective error vs HiGHS "
+          f"{abs(ci.primal_objective - entry['highs_objective']) / abs(entry['highs_objective']):.2e}")
+
+
+@pytest.mark.parametrize("entry", CONVERGE, ids=lambda e: f"seed{e['seed']}")
+def test_reduced_power_law_fp32_reaches_1e4(entry):
+    p = make(entry).problem
+    out = cupdlp.optimize(_params(tolerance=1e-4, precision=cupdlp.Precision.FP32), p)
+    assert out.termination_reason == OPT
+    ok, k = meets_tolerance(p, out.primal_solution, out.dual_solution, 1e-4, slack=1.05)
+    assert ok, k
+    # the objective error against the FP64 optimum that a 1e-4 relative gap permits
+    assert k["primal_objective"] == pytest.approx(entry["highs_objective"], rel=1e-3)
+
+
+def _reported_equals_recomputed(p, out, rtol):
+    ci = out.iteration_stats[-1].convergence_information[0]
+    ref = convergence_information(p, out.primal_solution, out.dual_solution, 1e-4, 1e-4)
+    for f in ("primal_objective", "dual_objective", "l2_primal_residual", "l2_dual_residual",
+              "l_inf_primal_residual", "l2_primal_variable", "l2_dual_variable", "relative_optimality_gap"):
+        assert getattr(ci, f) == pytest.approx(ref[f], rel=rtol, abs=1e-12), (f, getattr(ci, f), ref[f])
+
+
+@pytest.mark.parametrize("entry", STUDY, ids=lambda e: f"m{e['m']}")
+def test_reduced_power_law_budget_matches_oracle_state(entry):
+    """After the same 20,000-iteration budget the GPU is, like the oracle, far from 1e-4; its
+    reported statistics are those of its returned iterate."""
+    p = make(entry).problem
+    out = cupdlp.optimize(_params(tolerance=1e-4, iteration_limit=entry["budget"]), p)
+    assert out.termination_reason == LIMIT
+    ci = out.iteration_stats[-1].convergence_information[0]
+    g = entry["oracle_budget"]
+    # the trajectories differ by round-off amplification; the state is of the same order
+    assert 0.2 * g["relative_optimality_gap"] < ci.relative_optimality_gap < 5.0 * g["relative_optimality_gap"]
+    _reported_equals_recomputed(p, out, rtol=1e-9)
+
+
+@pytest.fixture(scope="module")
+def full_power_law():
+    return synthetic.power_law_lp()
+
+
+@pytest.mark.parametrize("precision", [cupdlp.Precision.FP32, cupdlp.Precision.FP64])
+def test_full_power_law_statistics_are_those_of_the_returned_iterate(full_power_law, precision):
+    p = full_power_law.problem
+    out = cupdlp.optimize(_params(tolerance=1e-4, iteration_limit=300, precision=precision), p)
+    assert out.termination_reason == LIMIT
+    # FP32 iterates are averaged in FP64 and returned as computed, so both agree to round-off
+    _reported_equals_recomputed(p, out, rtol=1e-6 if precision == cupdlp.Precision.FP32 else 1e-9)
