@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(kBlock, kPrimalCtasPerSm<T>) primal_step_kerne
       const Tile t = tl[q];
       load_in(t, E0);
       if (pending) {
-        tile_load(a.At.row_ptr, a.At.col, a.At.val, t, L0);
+        tile_load(a.At.row_ptr, a.plan.icol, a.plan.ival, t, L0);
         tile_sums(a.At.col, a.At.val, yg, t, L0, rs);
       }
       finish(t, E0);
@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualA
       const Tile t = tl[q];
       load_in(t, E0);
       if (!commit_only) {
-        tile_load(a.A.row_ptr, a.A.col, a.A.val, t, L0);
+        tile_load(a.A.row_ptr, a.plan.icol, a.plan.ival, t, L0);
         tile_sums(a.A.col, a.A.val, a.dx, t, L0, rs);
       }
       finish(t, E0);

@@ -15,22 +15,27 @@ struct TileLoad {
   T v[TileTraits<T>::kEMax];
 };
 
-// Issues the loads of tile t (none is used here, so all are in flight together).
+// Issues the loads of tile t (none is used here, so all are in flight together). The lane's
+// j-th column and value come from the plan's lane-interleaved copy (slot data_begin + 32 j +
+// lane), so each load instruction of the warp is one coalesced access; slots past the tile's
+// nonzeros are not read.
 template <class T>
-__device__ __forceinline__ void tile_load(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
-                                          const T* __restrict__ val, const Tile& t, TileLoad<T>& L) {
+__device__ __forceinline__ void tile_load(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ icol,
+                                          const T* __restrict__ ival, const Tile& t, TileLoad<T>& L) {
   if (t.e_log2 < 0) return;  // a long row: streamed by long_row_sum / group_row_sum
   const int lane = threadIdx.x & 31;
   const int E = 1 << t.e_log2;
   const int kb = lane << t.e_log2;
   const int ke = min(t.nnz, kb + E);
   L.rpl = lane <= t.rows ? row_ptr[t.row_begin + lane] : 0;
+  const int32_t* cp = icol + t.data_begin + lane;
+  const T* vp = ival + t.data_begin + lane;
 #pragma unroll
   for (int j = 0; j < TileTraits<T>::kEMax; ++j) {
     if (j >= E) break;  // E is the same for the whole warp: a uniform exit, nothing issued past it
     const bool in = kb + j < ke;
-    L.c[j] = in ? lds(col + t.nnz_begin + kb + j) : 0;
-    L.v[j] = in ? lds(val + t.nnz_begin + kb + j) : T(0);
+    L.c[j] = in ? lds(cp + 32 * j) : 0;
+    L.v[j] = in ? lds(vp + 32 * j) : T(0);
   }
 }
 

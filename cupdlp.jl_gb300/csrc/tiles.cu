@@ -11,6 +11,27 @@ int ceil_log2(long long v) {
   while ((1LL << l) < v) ++l;
   return l;
 }
+
+// One warp per warp tile: lane l's j-th nonzero (CSR position nnz_begin + l E + j) goes to
+// slot data_begin + 32 j + l; slots past the tile's nonzeros get column 0 and value 0.
+template <class T>
+__global__ void __launch_bounds__(256) interleave_tiles_kernel(const Tile* __restrict__ tiles, int ntiles,
+                                                              const int32_t* __restrict__ col,
+                                                              const T* __restrict__ val, int32_t* icol, T* ival) {
+  const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= ntiles) return;
+  const Tile t = tiles[w];
+  if (t.e_log2 < 0) return;
+  const int E = 1 << t.e_log2;
+  for (int j = 0; j < E; ++j) {
+    const int k = lane * E + j;
+    const long long dst = (long long)t.data_begin + 32LL * j + lane;
+    const bool in = k < t.nnz;
+    icol[dst] = in ? col[(long long)t.nnz_begin + k] : 0;
+    ival[dst] = in ? val[(long long)t.nnz_begin + k] : T(0);
+  }
+}
 }  // namespace
 
 void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t aux, int tile_nnz, int e_max,
@@ -116,6 +137,17 @@ void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector
   inst_cta[K] = (int32_t)cta_inst.size();
   inst_split[K] = splits;
   cta_begin.push_back((int32_t)tiles.size());
+  // slots of the lane-interleaved copy: 32 E per warp tile, in plan order
+  long long slots = 0;
+  for (Tile& t : tiles) {
+    if (t.e_log2 < 0) {
+      t.data_begin = 0;
+      continue;
+    }
+    t.data_begin = (int32_t)slots;
+    slots += 32LL << t.e_log2;
+    if (slots > 0x7fffffffLL) throw Error(GPDHG_ERR_NOT_SUPPORTED, "tile plan exceeds 2^31 interleaved slots");
+  }
   plan.num_tiles = (int32_t)tiles.size();
   plan.num_ctas = (int32_t)cta_inst.size();
   plan.num_splits = splits;
@@ -132,6 +164,18 @@ void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector
   plan.carry.alloc(std::max(carries, 1));
   plan.counter.alloc(std::max(splits, 1));
   CK(cudaMemsetAsync(plan.counter.get(), 0, sizeof(unsigned) * std::max(splits, 1), s));
+  plan.interleaved_slots = slots;
+  plan.icol.alloc(std::max<long long>(slots, 1));
+  plan.ival.alloc(std::max<long long>(slots, 1));
+  const CsrView<T> mv = M.view<T>();
+  if (M.nnz > 0 && !mv.val) throw Error(GPDHG_ERR_INTERNAL, "matrix values of the plan's precision are missing");
+  if (slots > 0) {
+    const int nt = plan.num_tiles;
+    const long long threads = 32LL * nt;
+    interleave_tiles_kernel<T><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+        plan.tiles.get(), nt, mv.col, mv.val, plan.icol.get(), plan.ival.get());
+    CK_LAUNCH();
+  }
   // the host vectors die at return: wait for the copies before they do
   CK(cudaStreamSynchronize(s));
 }

@@ -12,6 +12,15 @@
 // as make its CTAs a single wave over the GPU (no ragged last wave, and fewer partial sums
 // for the step decision to reduce). The decomposition depends only on the instance's own
 // row lengths, never on where the instance sits in a packed batch.
+//
+// Lane-interleaved copy: lane l of a warp tile owns the tile's nonzeros [l E, (l + 1) E)
+// (consecutive, so that rows are summed with one FMA per nonzero and few shuffles). Read
+// from the CSR, the j-th load of every lane would hit 32 addresses E elements apart. The plan
+// therefore keeps a copy of every warp tile's columns and values with the lane's j-th nonzero
+// at data_begin + 32 j + l: each of a lane's E loads is one coalesced 128-byte (FP32) or
+// 256-byte (FP64) access of the warp. Slots past the tile's nonzeros hold column 0 and value 0
+// and are never read. Long rows (warp-streamed, group and split) already stream the CSR
+// coalesced and have no copy.
 #pragma once
 
 #include <vector>
@@ -57,6 +66,7 @@ struct Tile {
   int32_t pieces;     // pieces of the split row
   int32_t carry;      // first carry slot of the split row
   int32_t aux;        // tiles of A: first inequality row of the instance (packed numbering)
+  int32_t data_begin; // warp tiles: first slot of the tile in the lane-interleaved copy
 };
 
 // Device view of a tile plan.
@@ -71,6 +81,8 @@ struct TileView {
   unsigned* counter;                // pieces finished per split row (back to 0 after each launch)
   const int32_t* cta_map;           // launched CTA -> plan CTA (NULL: the identity); a batch
                                     // launches only the CTAs of instances still running
+  const int32_t* icol;              // lane-interleaved columns of the warp tiles
+  const T* ival;                    // lane-interleaved values of the warp tiles
   int32_t num_ctas;
   int32_t num_splits;
 };
@@ -81,11 +93,14 @@ struct TilePlan {
   DBuf<int32_t> cta_tile_begin, cta_inst, inst_cta_begin, inst_split_begin;
   DBuf<T> carry;
   DBuf<unsigned> counter;
+  DBuf<int32_t> icol;
+  DBuf<T> ival;
   int32_t num_tiles = 0, num_ctas = 0, num_splits = 0;
+  long long interleaved_slots = 0;
   TileView<T> view() const {
     return TileView<T>{tiles.get(),      cta_tile_begin.get(), cta_inst.get(), inst_cta_begin.get(),
                        inst_split_begin.get(), carry.get(),     counter.get(),  nullptr,
-                       num_ctas,               num_splits};
+                       icol.get(),       ival.get(),            num_ctas,       num_splits};
   }
 };
 
@@ -95,7 +110,8 @@ void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t
                 std::vector<Tile>& out, int32_t& splits, int32_t& carries);
 
 // Plan of rows [bounds[k], bounds[k + 1]) for every instance k of matrix M (Tile::aux =
-// aux[k], or 0 when aux is empty).
+// aux[k], or 0 when aux is empty), with the lane-interleaved copy of M's precision-T values
+// (M.view<T>() must hold them).
 template <class T>
 void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector<int32_t>& bounds,
                      const std::vector<int32_t>& aux, int ctas_per_sm, cudaStream_t s);

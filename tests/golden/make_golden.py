@@ -15,7 +15,10 @@ The power-law section pins reduced instances of the large power-law generator: i
 optimum against HiGHS, and how many iterations the oracle needs (the family converges slowly
 under PDHG: most instances with m >= 1,000 do not reach 1e-4 within 300,000 iterations).
 
-Run:  python tests/golden/make_golden.py [--power-law-only]
+The full-size section holds the FP64 oracle's optimum of the transportation benchmark
+(1M columns) at 1e-8, the reference objective its benchmark result is measured against.
+
+Run:  python tests/golden/make_golden.py [--power-law-only | --full-size-only]
 """
 import hashlib
 import json
@@ -110,9 +113,32 @@ def power_law_entry(spec):
     return entry
 
 
+FULL_SIZE = {"transportation": {"gen": "transportation_lp", "seed": 1, "kw": {}}}
+
+
+def full_size_entry(spec):
+    p = make(spec).problem
+    entry = dict(spec)
+    entry["checksum"] = checksum(p)
+    for tol, key in ((1e-4, "oracle_1e4"), (1e-8, "oracle_1e8")):
+        res, x, y, st = oracle.optimize(p, cupdlp.default_parameters(tolerance=tol), max_stats=1000)
+        ci = res.last_iteration_stats.convergence_information
+        entry[key] = {"termination_reason": res.termination_reason, "iteration_count": res.iteration_count,
+                      "kkt_passes": res.cumulative_kkt_matrix_passes,
+                      "primal_objective": ci.primal_objective, "dual_objective": ci.dual_objective}
+    print(entry["gen"], entry["oracle_1e8"])
+    return entry
+
+
 def main():
     oracle.set_threads(8)
     path = os.path.join(HERE, "golden.json")
+    if "--full-size-only" in sys.argv:
+        out = json.load(open(path))
+        out["full_size"] = {k: full_size_entry(v) for k, v in FULL_SIZE.items()}
+        with open(path, "w") as f:
+            json.dump(out, f, indent=1)
+        return
     if "--power-law-only" in sys.argv:
         out = json.load(open(path))
         out["power_law"] = [power_law_entry(spec) for spec in POWER_LAW]
@@ -148,6 +174,7 @@ def main():
         out["instances"].append(entry)
         print(entry["gen"], entry["seed"], entry["highs_objective"], entry["oracle_1e8"])
     out["power_law"] = [power_law_entry(spec) for spec in POWER_LAW]
+    out["full_size"] = {k: full_size_entry(v) for k, v in FULL_SIZE.items()}
     with open(path, "w") as f:
         json.dump(out, f, indent=1)
 

@@ -161,3 +161,20 @@ def test_oracle_power_law_budget_state(entry, oracle_mod):
     assert ci.primal_objective == pytest.approx(g["primal_objective"], rel=1e-12)
     assert ci.relative_optimality_gap == pytest.approx(g["relative_optimality_gap"], rel=1e-10)
     assert ci.relative_optimality_gap > 0.1
+
+
+def test_transportation_full_size_golden(oracle_mod):
+    """The transportation benchmark (1M columns): the generator reproduces the committed
+    instance and the oracle its 1e-4 solve; the committed 1e-8 optimum (the reference objective
+    of the benchmark) is within the 1e-4 tolerance of the 1e-4 solve's objectives."""
+    g = GOLDEN["full_size"]["transportation"]
+    p = make(g).problem
+    assert checksum(p) == g["checksum"]
+    res, *_ = oracle_mod.optimize(p, cupdlp.default_parameters(tolerance=1e-4), max_stats=1000)
+    ci = res.last_iteration_stats.convergence_information
+    assert res.iteration_count == g["oracle_1e4"]["iteration_count"]
+    assert ci.primal_objective == pytest.approx(g["oracle_1e4"]["primal_objective"], rel=1e-12)
+    opt = g["oracle_1e8"]["primal_objective"]
+    assert g["oracle_1e8"]["dual_objective"] == pytest.approx(opt, rel=1e-8)
+    assert ci.primal_objective == pytest.approx(opt, rel=1e-4)
+    assert ci.dual_objective == pytest.approx(opt, rel=1e-4)
