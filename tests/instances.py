@@ -76,3 +76,21 @@ def long_rows_lp(seed=31, m=45000, n=45000, per_column=2, lengths=LONG_ROW_LENGT
     a.sum_duplicates()
     a.sort_indices()
     return synthetic._planted(rng, a, int(round(0.6 * m)), np.full(n, 10.0), f"long_rows_m{m}_n{n}_s{seed}")
+
+
+def infeasible_planted_lp(kind, seed=51, m=400, n=800, density=0.01):
+    """A planted-optimum LP made infeasible: kind "primal" repeats equality row 0 with its
+    right-hand side raised by 1 (two contradictory equalities); kind "dual" appends a column
+    with cost -1, no constraint coefficients and no upper bound (the objective is unbounded
+    below along it)."""
+    from cupdlp import synthetic
+    base = synthetic.known_optimum_lp(seed, m=m, n=n, density=density).problem
+    a = sp.csr_matrix(base.constraint_matrix)
+    l, u, c, b, neq = (base.variable_lower_bound, base.variable_upper_bound, base.objective_vector,
+                       base.right_hand_side, base.num_equalities)
+    if kind == "primal":
+        a = sp.vstack([a[:neq], a[0:1], a[neq:]], format="csc")
+        b = np.concatenate([b[:neq], [b[0] + 1.0], b[neq:]])
+        return lp(a, b, c, l, u, neq + 1)
+    a = sp.hstack([a, sp.csr_matrix((a.shape[0], 1))], format="csc")
+    return lp(a, b, np.append(c, -1.0), np.append(l, 0.0), np.append(u, np.inf), neq)

@@ -1,0 +1,73 @@
+"""InfeasibilityInformation parity (compute_infeasibility_information,
+src/iteration_stats_utils_gpu.jl:314-372; the fields of src/solve_log.jl:161-212) against
+the oracle, on feasible, primal-infeasible and dual-infeasible LPs: every field at every
+evaluation of the first 30 iterations to rtol 1e-9, and the termination reason and the last
+evaluation's ray statistics when the infeasibility is detected."""
+import pytest
+
+import cupdlp
+from cupdlp import synthetic
+
+import instances
+from test_gpu_parity import _params, _rel, solve_both
+
+pytestmark = pytest.mark.gpu
+
+RAY_FIELDS = ["max_primal_ray_infeasibility", "primal_ray_linear_objective", "max_dual_ray_infeasibility",
+              "dual_ray_objective"]
+PI = cupdlp.TERMINATION_REASON_PRIMAL_INFEASIBLE
+DI = cupdlp.TERMINATION_REASON_DUAL_INFEASIBLE
+
+
+def _close(g, o, rtol, atol):
+    return abs(g - o) <= atol or _rel(g, o) <= rtol
+
+
+def compare_rays(gpu_stats, orc, rtol, atol=1e-12):
+    assert len(gpu_stats) == len(orc.stats)
+    for k, (g, o) in enumerate(zip(gpu_stats, orc.stats)):
+        gi, oi = g.infeasibility_information[0], o.infeasibility_information
+        assert int(gi.candidate_type) == oi.candidate_type, k
+        for f in RAY_FIELDS:
+            assert _close(getattr(gi, f), getattr(oi, f), rtol, atol), (k, f, getattr(gi, f), getattr(oi, f))
+
+
+CASES = {
+    "feasible": lambda: synthetic.known_optimum_lp(0).problem,
+    "primal_infeasible": lambda: instances.infeasible_planted_lp("primal"),
+    "dual_infeasible": lambda: instances.infeasible_planted_lp("dual"),
+    "tiny_primal_infeasible": instances.primal_infeasible,
+    "tiny_dual_infeasible": instances.dual_infeasible,
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+@pytest.mark.parametrize("iters", [1, 10, 30])
+def test_ray_statistics_short_horizon(case, iters):
+    p = CASES[case]()
+    params = _params(tolerance=1e-10, iteration_limit=iters)
+    sq, (res, *rest), orc, _ = solve_both(p, params)
+    stats = rest[2]
+    assert res.termination_reason == orc.result.termination_reason
+    compare_rays(stats, orc, rtol=1e-9)
+
+
+@pytest.mark.parametrize("case,reason", [("primal_infeasible", PI), ("dual_infeasible", DI),
+                                         ("tiny_primal_infeasible", PI), ("tiny_dual_infeasible", DI)])
+def test_detected_infeasibility_matches_oracle(case, reason):
+    p = CASES[case]()
+    params = _params(tolerance=1e-6, iteration_limit=200000)
+    sq, (res, *rest), orc, _ = solve_both(p, params)
+    assert res.termination_reason == orc.result.termination_reason == reason
+    # the certificate is detected at an evaluation point; round-off may move it by a few
+    assert abs(res.iteration_count - orc.result.iteration_count) <= 0.5 * orc.result.iteration_count + 64
+    gi = res.last_iteration_stats.infeasibility_information
+    oi = orc.result.last_iteration_stats.infeasibility_information
+    if reason == PI:
+        # a dual ray: objective > 0 and infeasibility ~ 0 on both sides
+        assert gi.dual_ray_objective > 0 and oi.dual_ray_objective > 0
+        assert gi.max_dual_ray_infeasibility / gi.dual_ray_objective <= 1e-8
+    else:
+        # a primal ray: objective < 0 and infeasibility ~ 0 on both sides
+        assert gi.primal_ray_linear_objective < 0 and oi.primal_ray_linear_objective < 0
+        assert gi.max_primal_ray_infeasibility / -gi.primal_ray_linear_objective <= 1e-8
