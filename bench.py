@@ -28,6 +28,10 @@ problem resident in HBM. `--workload transportation` is the transportation LP (5
               fp64_pipe_active_pct_ncu come from the committed ncu capture (profiles/).
   cpu_baseline  the oracle (the CPU FP64 restatement of the reference loop) on the host
               cores: the same 1,000 iterations (power-law), the full solve (transportation).
+  reference_gpu_equiv  the reference's loop in its own GPU form on the same GPU
+              (baseline/ref_equiv.cu: cuSPARSE CSR_ALG2 FP64 SpMV, one kernel per reference
+              kernel or broadcast with the reference's synchronisations, dot / nrm2 read back by
+              the host every attempt), on the same problem, parameters and iteration budget.
 
 --impl reference times that CPU implementation alone (the reference itself is Julia
 and cannot be installed here). Multi-GPU: replicas only (a single LP does not shard).
@@ -297,6 +301,31 @@ def cpu_baseline(lp_problem, params, iters_cap, threads=None):
             "kkt_passes": r.cumulative_kkt_matrix_passes}
 
 
+def reference_gpu_equiv(sq, params, repeats=2):
+    """The reference-form GPU baseline on the same scaled problem: KKT passes / s of its solve
+    (host wall clock around its loop, as the reference times itself), best of `repeats`."""
+    sys.path.insert(0, os.path.join(REPO, "baseline"))
+    import cupdlp
+    import ref_equiv
+    p64 = cupdlp.default_parameters(tolerance=params.termination_criteria.eps_optimal_relative,
+                                    iteration_limit=params.termination_criteria.iteration_limit,
+                                    record_iteration_stats=False)
+    best = None
+    for _ in range(repeats):
+        r, _, _ = ref_equiv.solve_scaled(sq, p64, want_solution=False)
+        if best is None or r.solve_time_sec < best.solve_time_sec:
+            best = r
+    ci = best.last_iteration_stats.convergence_information
+    return best, {"value": best.cumulative_kkt_matrix_passes / best.solve_time_sec, "unit": "KKT passes/s",
+                  "solve_sec": best.solve_time_sec, "iterations": best.iteration_count,
+                  "kkt_passes": best.cumulative_kkt_matrix_passes, "termination": best.termination_reason,
+                  "primal_objective": ci.primal_objective, "kernels_per_iteration":
+                      best.kernels_launched / max(1, best.iteration_count),
+                  "form": "reference call pattern on this GPU: cuSPARSE CSR_ALG2 FP64 SpMV, per-kernel "
+                          "sync, host-side dot/nrm2 every attempt (baseline/ref_equiv.cu); best of "
+                          f"{repeats} solves"}
+
+
 def run_reference(args):
     world, rank, local, pg = dist_setup(args.gpus)
     if rank != 0:
@@ -368,6 +397,29 @@ def run_batch(args):
         with DeviceProblem(d) as dp:
             dp.solve(params, want_solution=False)
     seq = time.perf_counter() - t0
+    # the reference's loop in its own GPU form, one instance after another, on every 8th
+    # instance (a sample of the same size mix), FP64 as the reference computes
+    rge = None
+    if rank == 0:
+        try:
+            sys.path.insert(0, os.path.join(REPO, "baseline"))
+            import ref_equiv
+            p64 = cupdlp.default_parameters(tolerance=args.tolerance, record_iteration_stats=False,
+                                            time_sec_limit=600.0)
+            sample = list(range(0, len(scaled), 8))
+            t0 = time.perf_counter()
+            ok = 0
+            for k in sample:
+                r, _, _ = ref_equiv.solve_scaled(scaled[k], p64, want_solution=False)
+                ok += int(r.termination_reason == 1)
+            tr = time.perf_counter() - t0
+            rge = {"value": len(sample) / tr, "unit": "solves/s", "sample": f"{len(sample)} of {len(scaled)} "
+                   f"instances (every 8th), solved one after another, {tr:.1f} s", "terminated_optimal": ok,
+                   "ours_over_reference": value / world / (len(sample) / tr),
+                   "form": "reference call pattern on this GPU: cuSPARSE CSR_ALG2 FP64 SpMV, per-kernel sync, "
+                           "host-side dot/nrm2 every attempt (baseline/ref_equiv.cu)"}
+        except Exception as e:
+            rge = {"unavailable": f"{type(e).__name__}: {e}"}
     # e2e: the batched call with host buffers (pack + upload + solve + copy back)
     t0 = time.perf_counter()
     with DeviceBatch(descs) as dq:
@@ -389,6 +441,8 @@ def run_batch(args):
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches), "clocks": clocks,
     }
+    if rge:
+        line["reference_gpu_equiv"] = rge
     db.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -638,6 +692,17 @@ def run_ours(args):
         # the same work on both sides: time to the same result (tolerance or iteration budget)
         cb["gpu_speedup_time_to_result"] = cb["solve_sec"] / (t_max / args.steps)
 
+    # the reference's loop in its own GPU form, same problem and iteration budget (rank 0)
+    rge = None
+    if rank == 0:
+        try:
+            _, rge = reference_gpu_equiv(sq, params)
+            our_sec = t_max / args.steps
+            rge["ours_over_reference_kkt_rate"] = value / world / rge["value"]
+            rge["ours_over_reference_time_to_result"] = rge["solve_sec"] / our_sec
+        except Exception as e:   # the baseline is reported, never required
+            rge = {"unavailable": f"{type(e).__name__}: {e}"}
+
     r0 = results[-1]
     ci = r0.last_iteration_stats.convergence_information
     line = {
@@ -662,6 +727,8 @@ def run_ours(args):
     }
     if cb:
         line["cpu_baseline"] = cb
+    if rge:
+        line["reference_gpu_equiv"] = rge
     dp.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
