@@ -124,6 +124,10 @@ def objective_error(name, lp, ci):
             "relative_l2_dual_residual": ci.relative_l2_dual_residual}
 
 
+def precision_name(prec):
+    return {0: "FP64", 1: "FP32_REFINE", 2: "FP32"}.get(int(prec), str(prec))
+
+
 def bytes_model(m, n, nnz, prec):
     """Algorithmic bytes of the two step kernels (minimum traffic of the fused schedule,
     gathered vectors counted once)."""
@@ -609,8 +613,12 @@ def run_ours(args):
 
     def timed_solves(profile):
         # solves with the inputs resident, each bracketed by CUDA events on the problem's
-        # stream, L2 flushed before each
+        # stream, L2 flushed before each. The profiled solves of an FP32_REFINE workload run
+        # its FP32 bulk phase alone (plain FP32, same iterations), so that every profiled
+        # launch is an FP32 launch, the precision the byte model counts.
         cparams.profile_kernels = 1 if profile else 0
+        cparams.precision = int(cupdlp.Precision.FP32 if profile and prec == cupdlp.Precision.FP32_REFINE
+                                else prec)
         out, ms = [], 0.0
         for _ in range(args.steps):
             flush.zero_()
@@ -669,6 +677,8 @@ def run_ours(args):
                                        "dual_step_kernel": td / max(tp + td, 1e-30)},
                 "bytes_per_launch": {"primal_with_commit": bm["primal_commit"], "dual": bm["dual"]},
                 "fp64_pipe_active_pct_ncu": profile_fp64_pipe(args.workload, dom),
+                "profiled_precision": "FP32 (the bulk phase)" if prec == cupdlp.Precision.FP32_REFINE else
+                                      precision_name(prec),
                 "step_pair_GBps": ((bytes_p + bytes_d) / (tp + td) / 1e9) if tp + td > 0 else None}
 
     # e2e through the C ABI with host buffers (create -> solve -> copy back), every step
