@@ -18,7 +18,8 @@ under PDHG: most instances with m >= 1,000 do not reach 1e-4 within 300,000 iter
 The full-size section holds the FP64 oracle's optimum of the transportation benchmark
 (1M columns) at 1e-8, the reference objective its benchmark result is measured against.
 
-Run:  python tests/golden/make_golden.py [--power-law-only | --full-size-only]
+Run:  python tests/golden/make_golden.py [--power-law-only | --full-size-only |
+                                           --power-law-iterations-only]
 """
 import hashlib
 import json
@@ -55,6 +56,13 @@ POWER_LAW = [
     {"gen": "power_law_lp", "seed": 3, "kw": {"m": 300, "n": 600, "target_nnz": 3000}, "kind": "converge"},
     {"gen": "power_law_lp", "seed": 7, "kw": {"m": 2000, "n": 4000, "target_nnz": 40000}, "kind": "study",
      "budget": 20000},
+]
+# Iterations the oracle needs on the family as it grows (recorded, not re-run by the tests):
+# to 1e-4 and to 1e-8 within a cap of `budget` iterations.
+POWER_LAW_ITERATIONS = [
+    {"gen": "power_law_lp", "seed": s, "kw": {"m": m, "n": 2 * m, "target_nnz": 10 * m}, "budget": cap}
+    for (m, cap) in ((300, 300000), (1000, 300000), (3000, 300000), (20000, 100000))
+    for s in (1, 3, 5, 7)
 ]
 
 
@@ -130,9 +138,31 @@ def full_size_entry(spec):
     return entry
 
 
+def iterations_entry(spec):
+    p = make(spec).problem
+    entry = dict(spec)
+    entry["nnz"] = int(p.constraint_matrix.nnz)
+    for tol, key in ((1e-4, "tol_1e4"), (1e-8, "tol_1e8")):
+        res, x, y, st = oracle.optimize(p, cupdlp.default_parameters(tolerance=tol, iteration_limit=spec["budget"]),
+                                        max_stats=10)
+        ci = res.last_iteration_stats.convergence_information
+        entry[key] = {"termination_reason": res.termination_reason, "iteration_count": res.iteration_count,
+                      "relative_optimality_gap": ci.relative_optimality_gap}
+        if res.termination_reason != 1:
+            break
+    print(spec["kw"]["m"], spec["seed"], entry.get("tol_1e4"), entry.get("tol_1e8"), flush=True)
+    return entry
+
+
 def main():
     oracle.set_threads(8)
     path = os.path.join(HERE, "golden.json")
+    if "--power-law-iterations-only" in sys.argv:
+        out = json.load(open(path))
+        out["power_law_iterations"] = [iterations_entry(spec) for spec in POWER_LAW_ITERATIONS]
+        with open(path, "w") as f:
+            json.dump(out, f, indent=1)
+        return
     if "--full-size-only" in sys.argv:
         out = json.load(open(path))
         out["full_size"] = {k: full_size_entry(v) for k, v in FULL_SIZE.items()}
@@ -175,6 +205,7 @@ def main():
         print(entry["gen"], entry["seed"], entry["highs_objective"], entry["oracle_1e8"])
     out["power_law"] = [power_law_entry(spec) for spec in POWER_LAW]
     out["full_size"] = {k: full_size_entry(v) for k, v in FULL_SIZE.items()}
+    out["power_law_iterations"] = [iterations_entry(spec) for spec in POWER_LAW_ITERATIONS]
     with open(path, "w") as f:
         json.dump(out, f, indent=1)
 

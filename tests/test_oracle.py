@@ -178,3 +178,17 @@ def test_transportation_full_size_golden(oracle_mod):
     assert g["oracle_1e8"]["dual_objective"] == pytest.approx(opt, rel=1e-8)
     assert ci.primal_objective == pytest.approx(opt, rel=1e-4)
     assert ci.dual_objective == pytest.approx(opt, rel=1e-4)
+
+
+def test_power_law_iterations_record(oracle_mod):
+    """The recorded iterations-to-tolerance of the family (tests/golden, power_law_iterations):
+    the instances regenerate with the recorded sizes, and the cheapest record re-runs exactly."""
+    rec = GOLDEN["power_law_iterations"]
+    for e in rec:
+        assert make(e).problem.constraint_matrix.nnz == e["nnz"]
+    e = min((e for e in rec if e["tol_1e4"]["termination_reason"] == 1), key=lambda e: e["tol_1e4"]["iteration_count"])
+    res, *_ = oracle_mod.optimize(make(e).problem, cupdlp.default_parameters(tolerance=1e-4,
+                                                                                iteration_limit=e["budget"]), max_stats=10)
+    assert res.iteration_count == e["tol_1e4"]["iteration_count"]
+    # the family slows down as it grows: no instance with m >= 3,000 reaches 1e-4 within its budget
+    assert all(e["tol_1e4"]["termination_reason"] != 1 for e in rec if e["kw"]["m"] >= 3000)
