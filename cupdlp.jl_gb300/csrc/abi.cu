@@ -139,6 +139,7 @@ gpdhg_status gpdhg_solve(gpdhg_problem* p, const gpdhg_params* params, gpdhg_res
     if (!p || !result) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "problem or result is NULL");
     check_params(params);
     gpdhg::solve(p, *params, result, primal_out, dual_out);
+    gpdhg::to_caller_columns(p->col_perm, primal_out);
   });
 }
 
@@ -232,6 +233,7 @@ gpdhg_status gpdhg_get_rescaling(const gpdhg_problem* p, double* constraint_resc
   return guarded([&] {
     if (!p) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "problem is NULL");
     gpdhg::get_rescaling(p, constraint_rescaling, variable_rescaling);
+    gpdhg::to_caller_columns(p->col_perm, variable_rescaling);
   });
 }
 
@@ -249,7 +251,10 @@ gpdhg_status gpdhg_set_warm_start(gpdhg_problem* p, const double* x0, const doub
     if (!p) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "problem is NULL");
     p->warm_x.clear();
     p->warm_y.clear();
-    if (x0) p->warm_x.assign(x0, x0 + p->n);
+    if (x0) {
+      p->warm_x.assign(x0, x0 + p->n);
+      if (!p->col_perm.empty()) gpdhg::to_handle_columns(p->col_perm, x0, p->warm_x.data());
+    }
     if (y0) p->warm_y.assign(y0, y0 + p->m);
   });
 }
@@ -258,6 +263,7 @@ gpdhg_status gpdhg_get_current_iterate(const gpdhg_problem* p, double* x, double
   return guarded([&] {
     if (!p) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "problem is NULL");
     gpdhg::current_iterate(p, x, y);
+    gpdhg::to_caller_columns(p->col_perm, x);
   });
 }
 

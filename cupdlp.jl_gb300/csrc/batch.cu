@@ -90,6 +90,7 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
   B->norm_b.assign(count, 0.0);
   B->norm_c.assign(count, 0.0);
   B->neq.resize(count);
+  B->col_perm.assign(count, {});
   // every descriptor validated (on host threads, one instance each); the error of the first
   // invalid instance is the one reported, as a serial loop would
   for_each_instance(count, [&](int k) { validate_lp_desc(&descs[k], false); });
@@ -126,8 +127,17 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
       arp[ro + i + 1] = (int32_t)(z0 + d.row_ptr[i + 1]);
       ineq[ro + i] = i >= d.num_equalities;
     }
+    // the instance's column order, chosen from its column degrees as for a lone problem
+    std::vector<int32_t> degree((size_t)n, 0);
+    for (long long e = 0; e < d.nnz; ++e) ++degree[(size_t)d.col_idx[e]];
+    std::vector<int32_t>& perm = B->col_perm[k];
+    std::vector<int32_t> inv;
+    if (choose_column_order(degree, perm)) {
+      inv.resize((size_t)n);
+      for (int32_t q = 0; q < n; ++q) inv[(size_t)perm[(size_t)q]] = q;
+    }
     for (long long e = 0; e < d.nnz; ++e) {
-      acol[z0 + e] = d.col_idx[e] + co;
+      acol[z0 + e] = (inv.empty() ? d.col_idx[e] : inv[(size_t)d.col_idx[e]]) + co;
       aval[z0 + e] = d.values[e];
     }
     for (RowItem it : build_row_items(d.row_ptr, m))
@@ -138,16 +148,23 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
       if (p) std::copy(p, p + len, dst.begin() + off);
       else std::fill(dst.begin() + off, dst.begin() + off + len, 1.0);
     };
-    put(l, co, d.variable_lower_bound, nullptr, n);
-    put(u, co, d.variable_upper_bound, nullptr, n);
-    put(c, co, d.objective_vector, nullptr, n);
+    // n-vectors in the instance's column order
+    auto put_n = [&](std::vector<double>& dst, const double* src, const double* fb) {
+      const double* p = src ? src : fb;
+      if (!p) std::fill(dst.begin() + co, dst.begin() + co + n, 1.0);
+      else if (perm.empty()) std::copy(p, p + n, dst.begin() + co);
+      else to_handle_columns(perm, p, dst.data() + co);
+    };
+    put_n(l, d.variable_lower_bound, nullptr);
+    put_n(u, d.variable_upper_bound, nullptr);
+    put_n(c, d.objective_vector, nullptr);
     put(b, ro, d.right_hand_side, nullptr, m);
-    put(ol, co, d.original_variable_lower_bound, d.variable_lower_bound, n);
-    put(ou, co, d.original_variable_upper_bound, d.variable_upper_bound, n);
-    put(oc, co, d.original_objective_vector, d.objective_vector, n);
+    put_n(ol, d.original_variable_lower_bound, d.variable_lower_bound);
+    put_n(ou, d.original_variable_upper_bound, d.variable_upper_bound);
+    put_n(oc, d.original_objective_vector, d.objective_vector);
     put(ob, ro, d.original_right_hand_side, d.right_hand_side, m);
     put(con, ro, d.constraint_rescaling, nullptr, m);
-    put(var, co, d.variable_rescaling, nullptr, n);
+    put_n(var, d.variable_rescaling, nullptr);
     // host scalars (as problem_init)
     double amax = 0.0, nb = 0.0, nc = 0.0;
     for (int64_t e = 0; e < d.nnz; ++e) amax = std::max(amax, std::fabs(d.values[e]));
@@ -569,6 +586,7 @@ static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& 
             for (int q = 0; q < len; ++q) hdst[q] = (double)tmp[q];
           };
           fetch_slice(W.ax.get(), primal_out ? primal_out[k] : nullptr, B->col_off[k], B->col_off[k + 1] - B->col_off[k]);
+          if (primal_out) to_caller_columns(B->col_perm[k], primal_out[k]);
           fetch_slice(W.ay.get(), dual_out ? dual_out[k] : nullptr, B->row_off[k], B->row_off[k + 1] - B->row_off[k]);
           retired[k] = 1;
           fh[k] = 0;

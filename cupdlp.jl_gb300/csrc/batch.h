@@ -30,6 +30,7 @@ struct gpdhg_batch {
   std::vector<int32_t> row_off, col_off, neq;  // per instance (offsets: count + 1)
   std::vector<gpdhg::InstanceInfo> info;
   std::vector<double> amax, norm_b, norm_c;
+  std::vector<std::vector<int32_t>> col_perm;  // per instance: choose_column_order's order
   gpdhg::DeviceMatrix A, At;                   // block-diagonal CSR of A and A'
   gpdhg::DBuf<int32_t> row_off_d, neq_d;
   gpdhg::DBuf<double> l, u, c, b, ol, ou, oc, ob, con, var;

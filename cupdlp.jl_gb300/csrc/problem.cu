@@ -352,6 +352,7 @@ void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d) {
     upload_csr(p->A, d->num_constraints, d->num_variables, d->row_ptr, d->col_idx, d->values, s);
     transpose_on_device(p->A, p->At, s);
   });
+  apply_column_order(p);
 }
 
 namespace {
@@ -405,6 +406,7 @@ void problem_init_csc(gpdhg_problem* p, const gpdhg_lp_desc* d, const int64_t* c
     upload_csr(p->At, n, m, rp.data(), ri.data(), nz_val, s);
     transpose_on_device(p->At, p->A, s);
   });
+  apply_column_order(p);
 }
 
 void problem_init_two_sided(gpdhg_problem* p, const gpdhg_two_sided_desc* t, const int64_t* col_ptr,
@@ -530,6 +532,85 @@ void problem_init_two_sided(gpdhg_problem* p, const gpdhg_two_sided_desc* t, con
     transpose_on_device(At, p->A, s);
     if (!identity) transpose_on_device(p->A, At, s);
   });
+  apply_column_order(p);
+}
+
+bool choose_column_order(const std::vector<int32_t>& degree, std::vector<int32_t>& perm) {
+  const int32_t n = (int32_t)degree.size();
+  perm.clear();
+  if (n < kColumnOrderMinColumns) return false;
+  int32_t dmax = 0;
+  long long total = 0;
+  for (int32_t d : degree) {
+    dmax = std::max(dmax, d);
+    total += d;
+  }
+  if (total == 0) return false;
+  // counting sort by decreasing degree, stable: bucket starts from the largest degree down
+  std::vector<int64_t> start((size_t)dmax + 2, 0);
+  for (int32_t d : degree) ++start[(size_t)(dmax - d) + 1];
+  for (size_t q = 1; q < start.size(); ++q) start[q] += start[q - 1];
+  std::vector<int32_t> order((size_t)n);
+  for (int32_t j = 0; j < n; ++j) order[(size_t)start[(size_t)(dmax - degree[j])]++] = j;
+  const int32_t top = std::max<int32_t>(1, (n + 99) / 100);
+  long long top_nnz = 0;
+  for (int32_t k = 0; k < top; ++k) top_nnz += degree[order[k]];
+  if ((double)top_nnz < kColumnOrderTopShare * (double)total) return false;
+  perm.swap(order);
+  return true;
+}
+
+void to_caller_columns(const std::vector<int32_t>& perm, double* v) {
+  if (perm.empty() || !v) return;
+  std::vector<double> t(v, v + perm.size());
+  for (size_t k = 0; k < perm.size(); ++k) v[perm[k]] = t[k];
+}
+
+void to_handle_columns(const std::vector<int32_t>& perm, const double* in, double* out) {
+  for (size_t k = 0; k < perm.size(); ++k) out[k] = in[perm[k]];
+}
+
+namespace {
+__global__ void relabel_kernel(long long nnz, const int32_t* __restrict__ inv, int32_t* col) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nnz) col[k] = inv[col[k]];
+}
+__global__ void gather_kernel(int32_t n, const int32_t* __restrict__ perm, const double* __restrict__ src,
+                              double* __restrict__ dst) {
+  const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = src[perm[k]];
+}
+}  // namespace
+
+void apply_column_order(gpdhg_problem* p) {
+  const int32_t n = p->n;
+  std::vector<int32_t> degree((size_t)n);
+  for (int32_t j = 0; j < n; ++j) degree[(size_t)j] = p->At.host_rp[(size_t)j + 1] - p->At.host_rp[(size_t)j];
+  std::vector<int32_t> perm;
+  if (!choose_column_order(degree, perm)) return;
+  cudaStream_t s = p->stream;
+  std::vector<int32_t> inv((size_t)n);
+  for (int32_t k = 0; k < n; ++k) inv[(size_t)perm[(size_t)k]] = k;
+  DBuf<int32_t> dperm((size_t)n), dinv((size_t)n);
+  CK(cudaMemcpyAsync(dperm.get(), perm.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dinv.get(), inv.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+  if (p->A.nnz > 0) {
+    relabel_kernel<<<(unsigned)((p->A.nnz + 255) / 256), 256, 0, s>>>(p->A.nnz, dinv.get(), p->A.col.get());
+    CK_LAUNCH();
+  }
+  for (DBuf<double>* v : {&p->l, &p->u, &p->c, &p->ol, &p->ou, &p->oc, &p->var}) {
+    DBuf<double> t((size_t)n);
+    gather_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, dperm.get(), v->get(), t.get());
+    CK_LAUNCH();
+    std::swap(*v, t);
+    CK(cudaStreamSynchronize(s));   // t (the old vector) is freed at the end of this scope
+  }
+  // A' of the renumbered A: its rows are the columns in the new order, each listing its
+  // entries in increasing row as before; A keeps its row order and each row its entry order
+  transpose_on_device(p->A, p->At, s);
+  set_row_items(p->At, s);
+  CK(cudaStreamSynchronize(s));
+  p->col_perm.swap(perm);
 }
 
 void ensure_fp32_values(gpdhg_problem* p) {

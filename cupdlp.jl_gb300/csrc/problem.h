@@ -125,6 +125,9 @@ struct gpdhg_problem {
   // how many slack variables follow the caller's variables (empty / 0 otherwise)
   std::vector<int32_t> new_row_to_old;
   int32_t num_slacks = 0;
+  // column order inside the handle (column_order): handle column k is the caller's column
+  // col_perm[k]; empty when the handle keeps the caller's order
+  std::vector<int32_t> col_perm;
   ~gpdhg_problem();
 };
 
@@ -154,4 +157,23 @@ void ensure_fp32_values(gpdhg_problem* p);
 void rescale_on_device(gpdhg_problem* p, const gpdhg_params& prm);
 // Copies the constraint (m) and variable (n) rescaling vectors to the host.
 void get_rescaling(const gpdhg_problem* p, double* con, double* var);
+
+// Column order for the gathers of the dual step kernel (A dx gathers the primal candidate by
+// column index, one 32-byte sector per nonzero). When the column degrees are skewed (at least
+// kColumnOrderMinColumns columns, and the 1% most used columns hold at least
+// kColumnOrderTopShare of the nonzeros) the columns are renumbered by decreasing degree
+// (ties in the caller's order), so that the hot entries of the gathered vector share few
+// cache lines; otherwise the caller's order is kept. The choice depends only on the degrees,
+// so an LP gets the same order alone and inside a batch. Returns whether to renumber and
+// fills perm (new column k = old column perm[k]).
+constexpr int32_t kColumnOrderMinColumns = 1 << 16;
+constexpr double kColumnOrderTopShare = 0.2;
+bool choose_column_order(const std::vector<int32_t>& degree, std::vector<int32_t>& perm);
+// Renumbers the columns of a built problem by choose_column_order (A's column indices, A'
+// rebuilt, every n-vector permuted on the device) and records the order in col_perm.
+void apply_column_order(gpdhg_problem* p);
+// v (n entries, handle order) rewritten in the caller's column order, in place.
+void to_caller_columns(const std::vector<int32_t>& perm, double* v);
+// out[k] = in[perm[k]]: a caller-order vector in handle order.
+void to_handle_columns(const std::vector<int32_t>& perm, const double* in, double* out);
 }  // namespace gpdhg
