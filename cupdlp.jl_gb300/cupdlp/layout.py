@@ -1,5 +1,10 @@
 """Column order of an LP for the GPU's gathers (an addition; the reference has no counterpart).
 
+The library applies this order itself inside a problem handle when the column degrees are
+skewed (at least 65,536 columns, the 1% most used columns holding at least 20% of the
+nonzeros), and maps solutions back; this module is the same renumbering on the host, for
+callers who want the reordered LP itself.
+
 The dual step kernel gathers the primal candidate by column index once per nonzero. On a
 matrix with skewed column degrees (the power-law LP: the 1% most used columns hold 44% of
 the nonzeros) the hot entries are scattered over the whole vector, one 32-byte sector each.
