@@ -332,10 +332,6 @@ gpdhg_status gpdhg_server_submit(gpdhg_server* s, const gpdhg_lp_desc* desc, con
   return guarded([&] {
     if (!s || !desc || !ticket) throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "server, desc or ticket is NULL");
     check_params(params);
-    if (params->precision == GPDHG_PRECISION_FP32_REFINE)
-      throw gpdhg::Error(GPDHG_ERR_NOT_SUPPORTED, "served solves run in FP64 or FP32 (no FP64 hand-off)");
-    if (params->step_size_policy != GPDHG_STEPSIZE_ADAPTIVE)
-      throw gpdhg::Error(GPDHG_ERR_NOT_SUPPORTED, "served solves use the adaptive step size");
     *ticket = gpdhg::server_submit(s, *desc, *params);
   });
 }

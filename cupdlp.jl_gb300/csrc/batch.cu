@@ -450,7 +450,8 @@ struct BatchWorkspace {
 
 template <class T>
 static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& prm, gpdhg_result* results,
-                      double* const* primal_out, double* const* dual_out) {
+                      double* const* primal_out, double* const* dual_out,
+                      const std::function<void(int)>* on_retire) {
   cudaStream_t s = B->stream;
   const int K = B->count;
   const int N = B->N, M = B->M;
@@ -592,6 +593,8 @@ static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& 
           fh[k] = 0;
           st[k].done = 1;
           --alive;
+          r.kernels_launched = W.launches - launches0;
+          if (on_retire) (*on_retire)(k);
           continue;
         }
         if (st[k].count_primal > 0 && st[k].count_dual > 0) {
@@ -721,13 +724,13 @@ static void run_batch(gpdhg_batch* B, BatchWorkspace<T>& W, const gpdhg_params& 
 }
 
 void batch_solve(gpdhg_batch* B, const gpdhg_params& prm, gpdhg_result* results, double* const* primal_out,
-                 double* const* dual_out) {
+                 double* const* dual_out, const std::function<void(int)>* on_retire) {
   if (prm.precision == GPDHG_PRECISION_FP64) {
     if (!B->ws64) B->ws64.reset(new BatchWorkspace<double>(B));
-    run_batch(B, *B->ws64, prm, results, primal_out, dual_out);
+    run_batch(B, *B->ws64, prm, results, primal_out, dual_out, on_retire);
   } else {
     if (!B->ws32) B->ws32.reset(new BatchWorkspace<float>(B));
-    run_batch(B, *B->ws32, prm, results, primal_out, dual_out);
+    run_batch(B, *B->ws32, prm, results, primal_out, dual_out, on_retire);
   }
 }
 

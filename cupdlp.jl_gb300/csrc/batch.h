@@ -1,6 +1,8 @@
 // batch.h — the packed multi-LP layout behind gpdhg_batch.
 #pragma once
 
+#include <functional>
+
 #include <memory>
 #include <string>
 #include <vector>
@@ -47,8 +49,10 @@ struct gpdhg_batch {
 
 namespace gpdhg {
 void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs);
+// on_retire (optional) is called with an instance's index right after that instance has
+// terminated and its result and solution have been written (from the calling thread).
 void batch_solve(gpdhg_batch* B, const gpdhg_params& prm, gpdhg_result* results, double* const* primal_out,
-                 double* const* dual_out);
+                 double* const* dual_out, const std::function<void(int)>* on_retire = nullptr);
 
 // Serving loop (server.cu).
 double footprint_bytes(const gpdhg_lp_desc& d, const gpdhg_params& p);

@@ -138,6 +138,8 @@ namespace gpdhg {
 void validate_lp_desc(const gpdhg_lp_desc* d, bool threads);
 // Builds the device problem from a descriptor (throws gpdhg::Error).
 void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d);
+// The solve loop (solver.cu); primal_out in the handle's column order.
+void solve(gpdhg_problem* P, const gpdhg_params& prm, gpdhg_result* res, double* primal_out, double* dual_out);
 // The same from the matrix in compressed sparse columns (index base 0 or 1, int64 indices, as
 // Julia's SparseMatrixCSC): CSC(A) is uploaded as CSR(A') and A is built on the device.
 void problem_init_csc(gpdhg_problem* p, const gpdhg_lp_desc* d, const int64_t* col_ptr, const int64_t* row_val,

@@ -5,15 +5,20 @@
 // head request's parameters, as many as the admission limits allow (device footprint within
 // the HBM budget, resident request count, cohort size), after lingering briefly for more.
 // The cohort is packed into one segmented batch and solved; every instance retires from the
-// device work the moment it terminates, and the cohort's memory returns to the budget when
-// its last instance is done. Cohorts of different workers run concurrently, so a request
-// that arrives while others are on the GPU starts as soon as a worker and memory are free
-// and its kernels overlap with theirs. Each result is the lone solve's result bit for bit.
+// device work the moment it terminates, and its result is handed out at that moment (a
+// small request does not wait for the large ones it was packed with). The cohort's memory
+// returns to the budget when its last instance is done: the packed buffers are freed
+// together. Cohorts of different workers run concurrently, so a request that arrives while
+// others are on the GPU starts as soon as a worker and memory are free and its kernels
+// overlap with theirs. Each result is the lone solve's result bit for bit. Requests whose
+// parameters a batch does not take (the FP64 hand-off of FP32_REFINE, the constant step
+// size) are solved one after another as lone problems by the worker that picked them.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -79,13 +84,22 @@ bool same_params(const gpdhg_params& a, const gpdhg_params& b) { return std::mem
 // vectors (scaled and original, rescaling) and the workspace iterates.
 double footprint_bytes(const gpdhg_lp_desc& d, const gpdhg_params& p) {
   const double n = d.num_variables, m = d.num_constraints, z = (double)d.nnz;
-  const double t = p.precision == GPDHG_PRECISION_FP64 ? 8.0 : 4.0;
+  const bool fp64 = p.precision == GPDHG_PRECISION_FP64, refine = p.precision == GPDHG_PRECISION_FP32_REFINE;
+  const double t = fp64 ? 8.0 : 4.0;
   double bytes = 2.0 * (z * 12.0 + 4.0 * (n + m + 2.0));  // A and A' CSR
-  if (t == 4.0) bytes += 2.0 * z * 4.0;                   // FP32 values
-  bytes += 2.0 * 40.0 * (z / 32.0 + (n + m) / 16.0 + 2.0);  // tiles (generous)
+  if (!fp64) bytes += 2.0 * z * 4.0;                      // FP32 values
+  const double plans = refine ? 2.0 : 1.0;                // FP32_REFINE: an FP64 plan too
+  bytes += plans * 2.0 * 44.0 * (z / 32.0 + (n + m) / 16.0 + 2.0);  // tiles (generous)
+  bytes += plans * 2.0 * z * (t + 4.0) * 1.5;              // lane-interleaved tile copies
   bytes += 8.0 * (7.0 * n + 3.0 * m) + m + 4.0 * (n + m);  // FP64 vectors, flags, instance maps
   bytes += t * (13.0 * n + 11.0 * m);                      // workspace iterates
+  if (refine) bytes += 8.0 * (13.0 * n + 11.0 * m);        // the FP64 phase's workspace
   return 1.1 * bytes + (1 << 20);
+}
+
+// Parameters a batch takes (the rest is served by lone solves).
+bool batch_takes(const gpdhg_params& p) {
+  return p.precision != GPDHG_PRECISION_FP32_REFINE && p.step_size_policy == GPDHG_STEPSIZE_ADAPTIVE;
 }
 
 class Server {
@@ -208,7 +222,8 @@ class Server {
           continue;
         }
       }
-      solve(cohort);
+      if (batch_takes(cohort.front()->params)) solve(cohort);
+      else solve_alone(cohort);
       {
         std::lock_guard<std::mutex> lk(mu_);
         in_use_ -= fp;
@@ -236,10 +251,22 @@ class Server {
     gpdhg_status status = GPDHG_OK;
     std::string error;
     gpdhg_batch* b = nullptr;
+    // an instance's result is handed out as soon as it has terminated
+    const std::function<void(int)> retire = [&](int q) {
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        Request& r = *cohort[q];
+        r.status = GPDHG_OK;
+        r.result = results[q];
+        r.done = true;
+      }
+      cv_done_.notify_all();
+    };
     try {
       b = new gpdhg_batch();
       batch_init(b, k, descs.data());
-      batch_solve(b, cohort.front()->params, results.data(), xs.data(), ys.data());
+      for (int q = 0; q < k; ++q) cohort[q]->lp = HostLp();   // packed on the device: the copy can go
+      batch_solve(b, cohort.front()->params, results.data(), xs.data(), ys.data(), &retire);
     } catch (const Error& e) {
       status = e.status;
       error = e.what();
@@ -251,12 +278,52 @@ class Server {
       error = e.what();
     }
     delete b;
+    std::lock_guard<std::mutex> lk(mu_);
     for (int q = 0; q < k; ++q) {
       Request& r = *cohort[q];
-      r.status = status;
-      r.error = error;
-      r.result = results[q];
-      r.lp = HostLp();  // the LP is no longer needed
+      if (r.done) continue;   // handed out at its retirement
+      r.status = status == GPDHG_OK ? GPDHG_ERR_INTERNAL : status;
+      r.error = status == GPDHG_OK ? "the batch ended before this instance terminated" : error;
+      r.lp = HostLp();
+    }
+  }
+
+  // Requests a batch does not take: each solved as a lone problem, its result handed out
+  // when it is done.
+  void solve_alone(std::vector<std::shared_ptr<Request>>& cohort) {
+    for (auto& rp : cohort) {
+      Request& r = *rp;
+      r.x.assign((size_t)r.lp.d.num_variables, 0.0);
+      r.y.assign((size_t)r.lp.d.num_constraints, 0.0);
+      gpdhg_status status = GPDHG_OK;
+      std::string error;
+      gpdhg_result result{};
+      gpdhg_problem* p = nullptr;
+      try {
+        p = new gpdhg_problem();
+        problem_init(p, &r.lp.d);
+        gpdhg::solve(p, r.params, &result, r.x.data(), r.y.empty() ? nullptr : r.y.data());
+        to_caller_columns(p->col_perm, r.x.data());
+      } catch (const Error& e) {
+        status = e.status;
+        error = e.what();
+      } catch (const std::bad_alloc&) {
+        status = GPDHG_ERR_OUT_OF_MEMORY;
+        error = "host allocation failed";
+      } catch (const std::exception& e) {
+        status = GPDHG_ERR_INTERNAL;
+        error = e.what();
+      }
+      delete p;
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        r.status = status;
+        r.error = error;
+        r.result = result;
+        r.lp = HostLp();
+        r.done = true;
+      }
+      cv_done_.notify_all();
     }
   }
 

@@ -413,10 +413,13 @@ gpdhg_status gpdhg_convergence_noalloc(int32_t num_variables, int32_t num_constr
  * resident requests stays within hbm_budget_bytes and at most max_resident requests are
  * resident, so requests arriving while others run start as soon as memory and a worker
  * are free, and their kernels overlap with the running cohorts' on the device. An instance
- * that terminates stops launching work at once; its cohort's memory is released when the
- * cohort's last instance terminates. Each result is bit-identical to solving the same LP
- * alone with the same parameters (a batch gives every instance the same arithmetic as a
- * lone solve). Zero config fields take the defaults in brackets.
+ * that terminates stops launching work at once and its result can be collected at that
+ * moment; its cohort's memory is released when the cohort's last instance terminates.
+ * Requests whose parameters a batch does not take (FP32_REFINE with its FP64 hand-off, the
+ * constant step size) are solved one after another as lone problems by the worker that picks
+ * them. Each result is bit-identical to solving the same LP alone with the same parameters
+ * (a batch gives every instance the same arithmetic as a lone solve). Zero config fields
+ * take the defaults in brackets.
  * ------------------------------------------------------------------------------- */
 typedef struct gpdhg_server gpdhg_server;
 
@@ -433,8 +436,7 @@ typedef struct gpdhg_server_config {
 /* Estimated device bytes one request occupies while resident (the admission measure). */
 double gpdhg_server_footprint(const gpdhg_lp_desc* desc, const gpdhg_params* params);
 gpdhg_status gpdhg_server_create(const gpdhg_server_config* cfg, gpdhg_server** out);
-/* Copies the request; `ticket` identifies it. GPDHG_ERR_ADMISSION if it can never fit.
- * The parameters must be batchable: FP64 or FP32 precision, adaptive step size. */
+/* Copies the request; `ticket` identifies it. GPDHG_ERR_ADMISSION if it can never fit. */
 gpdhg_status gpdhg_server_submit(gpdhg_server* s, const gpdhg_lp_desc* desc, const gpdhg_params* params,
                                  uint64_t* ticket);
 /* Non-blocking: GPDHG_ERR_NOT_READY until the request has terminated. A request's result

@@ -90,7 +90,40 @@ def test_admission_and_ticket_lifecycle():
         with pytest.raises(cupdlp._abi.GpdhgError) as e:   # a ticket is handed out once
             srv.wait(t, timeout=1.0)
         assert e.value.status == cupdlp._abi.ERR_INVALID_ARGUMENT
-        # FP32_REFINE cannot be served (no hand-off inside a batch)
-        with pytest.raises(cupdlp._abi.GpdhgError) as e:
-            srv.submit(d, _params(cupdlp.Precision.FP32_REFINE, 1e-6))
-        assert e.value.status == cupdlp._abi.ERR_NOT_SUPPORTED
+
+
+def test_fp32_refine_and_constant_step_requests_are_served_alone():
+    """A batch has no FP64 hand-off and only the adaptive step size; such requests are
+    solved as lone problems by the worker and equal the lone solve bit for bit."""
+    scaled = _stream(34, 4)
+    p_ref = _params(cupdlp.Precision.FP32_REFINE, 1e-7)
+    p_const = _params(cupdlp.Precision.FP64, 1e-6)
+    p_const.step_size_policy_params = cupdlp.ConstantStepsizeParams()
+    with Server(workers=2, max_cohort=4) as srv:
+        plist = [p_ref, p_const, p_ref, _params(cupdlp.Precision.FP64, 1e-6)]
+        tickets = [srv.submit(scaled_desc(sq), p) for sq, p in zip(scaled, plist)]
+        served = [srv.wait(t, timeout=600.0) for t in tickets]
+    for k, (sq, p) in enumerate(zip(scaled, plist)):
+        _same(served[k], _alone(sq, p), k)
+    assert served[0][0].fp64_handoff_iteration > 0
+
+
+def test_results_are_handed_out_as_each_instance_terminates():
+    """Requests packed into one cohort: the quick ones' results are collected while the slow
+    one (a power-law LP that runs to the 60,000-iteration limit) is still on the device, and
+    all equal their lone solves."""
+    big = cupdlp.rescale_problem(10, False, 1.0, 0, synthetic.power_law_lp(1, m=300, n=600,
+                                                                          target_nnz=3000).problem)
+    small = [cupdlp.rescale_problem(10, False, 1.0, 0, synthetic.known_optimum_lp(36 + k, m=60, n=120,
+                                                                                  density=0.05).problem)
+             for k in range(3)]
+    params = _params(cupdlp.Precision.FP64, 1e-8)
+    with Server(workers=1, max_cohort=4, linger_sec=0.05) as srv:
+        tickets = [srv.submit(scaled_desc(sq), params) for sq in [big] + small]
+        got_small = [srv.wait(t, timeout=600.0) for t in tickets[1:]]
+        big_pending = srv.poll(tickets[0]) is None
+        got_big = srv.wait(tickets[0], timeout=600.0)
+    assert big_pending
+    for k, sq in enumerate(small):
+        _same(got_small[k], _alone(sq, params), k)
+    _same(got_big, _alone(big, params), "big")
