@@ -136,9 +136,24 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
       inv.resize((size_t)n);
       for (int32_t q = 0; q < n; ++q) inv[(size_t)perm[(size_t)q]] = q;
     }
-    for (long long e = 0; e < d.nnz; ++e) {
-      acol[z0 + e] = (inv.empty() ? d.col_idx[e] : inv[(size_t)d.col_idx[e]]) + co;
-      aval[z0 + e] = d.values[e];
+    if (inv.empty()) {
+      for (long long e = 0; e < d.nnz; ++e) {
+        acol[z0 + e] = d.col_idx[e] + co;
+        aval[z0 + e] = d.values[e];
+      }
+    } else {
+      // renumbered columns, each row re-sorted by its new column (ties in their previous
+      // order), as apply_column_order leaves a lone problem
+      std::vector<std::pair<int32_t, double>> row;
+      for (int32_t i = 0; i < m; ++i) {
+        row.clear();
+        for (int32_t e = d.row_ptr[i]; e < d.row_ptr[i + 1]; ++e) row.emplace_back(inv[(size_t)d.col_idx[e]], d.values[e]);
+        std::stable_sort(row.begin(), row.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+        for (size_t q = 0; q < row.size(); ++q) {
+          acol[z0 + d.row_ptr[i] + (long long)q] = row[q].first + co;
+          aval[z0 + d.row_ptr[i] + (long long)q] = row[q].second;
+        }
+      }
     }
     for (RowItem it : build_row_items(d.row_ptr, m))
       a_items_of[k].push_back({it.row_begin + ro, it.row_end + ro, it.group, it.mode, it.nnz_begin + (int32_t)z0, it.nnz_count});

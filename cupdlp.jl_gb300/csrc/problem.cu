@@ -605,9 +605,12 @@ void apply_column_order(gpdhg_problem* p) {
     std::swap(*v, t);
     CK(cudaStreamSynchronize(s));   // t (the old vector) is freed at the end of this scope
   }
-  // A' of the renumbered A: its rows are the columns in the new order, each listing its
-  // entries in increasing row as before; A keeps its row order and each row its entry order
+  // A' of the renumbered A (its rows are the columns in the new order, each listing its
+  // entries in increasing row as before), then A again from A', so that every row of A lists
+  // its entries in increasing new column (the layout a caller's own sorted CSR of the
+  // renumbered LP gives, ties in their previous order)
   transpose_on_device(p->A, p->At, s);
+  transpose_on_device(p->At, p->A, s);
   set_row_items(p->At, s);
   CK(cudaStreamSynchronize(s));
   p->col_perm.swap(perm);

@@ -171,8 +171,9 @@ void get_rescaling(const gpdhg_problem* p, double* con, double* var);
 constexpr int32_t kColumnOrderMinColumns = 1 << 16;
 constexpr double kColumnOrderTopShare = 0.2;
 bool choose_column_order(const std::vector<int32_t>& degree, std::vector<int32_t>& perm);
-// Renumbers the columns of a built problem by choose_column_order (A's column indices, A'
-// rebuilt, every n-vector permuted on the device) and records the order in col_perm.
+// Renumbers the columns of a built problem by choose_column_order (A's column indices, each
+// row of A re-sorted by its new column, A' rebuilt, every n-vector permuted on the device)
+// and records the order in col_perm.
 void apply_column_order(gpdhg_problem* p);
 // v (n entries, handle order) rewritten in the caller's column order, in place.
 void to_caller_columns(const std::vector<int32_t>& perm, double* v);
