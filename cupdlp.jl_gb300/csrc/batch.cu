@@ -184,7 +184,9 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
     double amax = 0.0, nb = 0.0, nc = 0.0;
     for (int64_t e = 0; e < d.nnz; ++e) amax = std::max(amax, std::fabs(d.values[e]));
     for (int32_t i = 0; i < m; ++i) nb += d.right_hand_side[i] * d.right_hand_side[i];
-    for (int32_t j = 0; j < n; ++j) nc += d.objective_vector[j] * d.objective_vector[j];
+    // column sums in the instance's column order, as apply_column_order has them
+    auto col = [&](int32_t j) { return perm.empty() ? j : perm[(size_t)j]; };
+    for (int32_t j = 0; j < n; ++j) nc += d.objective_vector[col(j)] * d.objective_vector[col(j)];
     B->amax[k] = amax;
     B->norm_b[k] = std::sqrt(nb);
     B->norm_c[k] = std::sqrt(nc);
@@ -193,7 +195,7 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
     InstanceInfo& qi = B->info[k];
     qi.obj_const = d.objective_constant;
     double s2 = 0.0, si = 0.0;
-    for (int32_t j = 0; j < n; ++j) { s2 += occ[j] * occ[j]; si = std::max(si, std::fabs(occ[j])); }
+    for (int32_t j = 0; j < n; ++j) { s2 += occ[col(j)] * occ[col(j)]; si = std::max(si, std::fabs(occ[col(j)])); }
     qi.l2_c = std::sqrt(s2); qi.linf_c = si;
     s2 = 0.0; si = 0.0;
     for (int32_t i = 0; i < m; ++i) { s2 += obb[i] * obb[i]; si = std::max(si, std::fabs(obb[i])); }

@@ -612,7 +612,14 @@ void apply_column_order(gpdhg_problem* p) {
   transpose_on_device(p->A, p->At, s);
   transpose_on_device(p->At, p->A, s);
   set_row_items(p->At, s);
+  // the 2-norms over the columns are summed in the new order (an LP whose caller already
+  // sorted its columns gets the same scalars, bit for bit)
+  std::vector<double> hc((size_t)n), hoc((size_t)n);
+  CK(cudaMemcpyAsync(hc.data(), p->c.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(hoc.data(), p->oc.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  p->norm2_c_scaled = norm2(hc.data(), n);
+  p->l2_c = norm2(hoc.data(), n);
   p->col_perm.swap(perm);
 }
 
