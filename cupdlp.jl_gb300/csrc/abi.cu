@@ -8,6 +8,7 @@
 
 #include "batch.h"
 #include "problem.h"
+#include "tiles.h"
 
 namespace gpdhg {
 void solve(gpdhg_problem* P, const gpdhg_params& prm, gpdhg_result* res, double* primal_out, double* dual_out);
@@ -268,6 +269,20 @@ gpdhg_status gpdhg_get_current_iterate(const gpdhg_problem* p, double* x, double
 }
 
 void* gpdhg_problem_stream(const gpdhg_problem* p) { return p ? (void*)p->stream : nullptr; }
+
+gpdhg_status gpdhg_set_tile_override(int32_t precision, int32_t side, int32_t tile_nnz, int32_t e_floor,
+                                     int32_t tpc_max) {
+  return guarded([&] {
+    if (precision != GPDHG_PRECISION_FP64 && precision != GPDHG_PRECISION_FP32)
+      throw gpdhg::Error(GPDHG_ERR_INVALID_ARGUMENT, "precision must be FP64 or FP32");
+    if (tile_nnz == 0) {
+      gpdhg::set_tile_override(precision, side, nullptr);
+      return;
+    }
+    const gpdhg::TileConfig c{tile_nnz, e_floor, tpc_max};
+    gpdhg::set_tile_override(precision, side, &c);
+  });
+}
 
 gpdhg_status gpdhg_batch_create(int32_t count, const gpdhg_lp_desc* descs, gpdhg_batch** out) {
   return guarded([&] {

@@ -335,10 +335,10 @@ struct BatchWorkspace {
     launch_reciprocal(B->con.get(), rcon.get(), M, s);
     st_dev.alloc(count);
     CK(cudaMemsetAsync(st_dev.get(), 0, sizeof(StepState) * count, s));
-    build_tile_plan(plan_p, B->At, B->col_off, {}, kPrimalCtasPerSm<T>, s);
+    build_tile_plan(plan_p, B->At, B->col_off, {}, kPrimalCtasPerSm<T>, kTileSideAt, s);
     std::vector<int32_t> ineq_from(count);
     for (int k = 0; k < count; ++k) ineq_from[k] = B->row_off[k] + B->neq[k];
-    build_tile_plan(plan_d, B->A, B->row_off, ineq_from, kDualCtasPerSm, s);
+    build_tile_plan(plan_d, B->A, B->row_off, ineq_from, kDualCtasPerSm, kTileSideA, s);
     part_p.alloc(plan_p.num_ctas);
     part_d.alloc(2 * (size_t)plan_d.num_ctas);
     part_p_split.alloc(std::max(plan_p.num_splits, 1));

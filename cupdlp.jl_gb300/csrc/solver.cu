@@ -162,7 +162,7 @@ struct Workspace {
     std::thread plan_thread([&] {
       try {
         CK(cudaSetDevice(device));   // a new host thread starts on device 0
-        build_tile_plan(plan_p, P->At, {0, n}, {}, kPrimalCtasPerSm<T>, s);
+        build_tile_plan(plan_p, P->At, {0, n}, {}, kPrimalCtasPerSm<T>, kTileSideAt, s);
       } catch (...) {
         plan_err = std::current_exception();
       }
@@ -176,7 +176,7 @@ struct Workspace {
       launch_reciprocal(P->con.get(), rcon.get(), m, s);
       st_dev.alloc(1);
       CK(cudaMemsetAsync(st_dev.get(), 0, sizeof(StepState), s));
-      build_tile_plan(plan_d, P->A, {0, m}, {P->neq}, kDualCtasPerSm, s);
+      build_tile_plan(plan_d, P->A, {0, m}, {P->neq}, kDualCtasPerSm, kTileSideA, s);
     } catch (...) {
       plan_thread.join();
       throw;

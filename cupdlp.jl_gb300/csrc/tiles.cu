@@ -1,6 +1,9 @@
 // tiles.cu — host builder of the tile plans of the step kernels.
 #include <algorithm>
+#include <cmath>
+#include <mutex>
 
+#include "tile_table.h"
 #include "tiles.h"
 
 namespace gpdhg {
@@ -33,6 +36,76 @@ __global__ void __launch_bounds__(256) interleave_tiles_kernel(const Tile* __res
   }
 }
 }  // namespace
+
+void row_histogram(const int32_t* rp, int32_t r0, int32_t r1, float* h) {
+  double w[kHistBins] = {};
+  long long total = 0;
+  for (int32_t r = r0; r < r1; ++r) {
+    const long long len = (long long)rp[r + 1] - rp[r];
+    if (len <= 0) continue;
+    int b = 0;
+    while (b < kHistBins - 1 && (2LL << b) <= len) ++b;
+    w[b] += (double)len;
+    total += len;
+  }
+  for (int b = 0; b < kHistBins; ++b) h[b] = total ? (float)(w[b] / (double)total) : 0.0f;
+  h[kHistBins] = total ? (float)(std::log2((double)total) / 32.0) : 0.0f;
+}
+
+template <class T>
+TileConfig default_tile_config() {
+  return TileConfig{TileTraits<T>::kNnz, TileTraits<T>::kEMax, kTilesPerCtaMax};
+}
+
+namespace {
+std::mutex g_override_mutex;
+bool g_override_set[2][2] = {};
+TileConfig g_override[2][2];
+int precision_slot(int precision) { return precision == GPDHG_PRECISION_FP64 ? 0 : 1; }
+}  // namespace
+
+void set_tile_override(int precision, int side, const TileConfig* cfg) {
+  if (side != kTileSideAt && side != kTileSideA) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "side must be 0 or 1");
+  std::lock_guard<std::mutex> lk(g_override_mutex);
+  const int q = precision_slot(precision);
+  g_override_set[q][side] = cfg != nullptr;
+  if (cfg) g_override[q][side] = *cfg;
+}
+
+template <class T>
+TileConfig choose_tile_config(const int32_t* rp, int32_t r0, int32_t r1, int side) {
+  const int q = sizeof(T) == 8 ? 0 : 1;
+  auto clamp = [](TileConfig c) {
+    c.tile_nnz = std::max(32, std::min(c.tile_nnz, TileTraits<T>::kNnz));
+    c.e_floor = std::max(1, std::min(c.e_floor, TileTraits<T>::kEMax));
+    c.tpc_max = std::max(kTilesPerCtaMin, std::min(c.tpc_max, kTilesPerCtaMax));
+    return c;
+  };
+  {
+    std::lock_guard<std::mutex> lk(g_override_mutex);
+    if (g_override_set[q][side]) return clamp(g_override[q][side]);
+  }
+  float h[kHistLen];
+  row_histogram(rp, r0, r1, h);
+  const TileTableEntry* best = nullptr;
+  double best_d = 0.0;
+  for (const TileTableEntry& e : kTileTable) {
+    if (e.fp64 != (q == 0) || e.side != side) continue;
+    double d = 0.0;
+    for (int b = 0; b < kHistLen; ++b) d += std::fabs((double)e.hist[b] - (double)h[b]);
+    if (!best || d < best_d) {
+      best = &e;
+      best_d = d;
+    }
+  }
+  if (!best) return default_tile_config<T>();
+  return clamp(TileConfig{best->tile_nnz, best->e_floor, best->tpc_max});
+}
+
+template TileConfig default_tile_config<float>();
+template TileConfig default_tile_config<double>();
+template TileConfig choose_tile_config<float>(const int32_t*, int32_t, int32_t, int);
+template TileConfig choose_tile_config<double>(const int32_t*, int32_t, int32_t, int);
 
 void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t aux, int tile_nnz, int e_max,
                 std::vector<Tile>& out, int32_t& splits, int32_t& carries) {
@@ -97,7 +170,7 @@ void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t
 
 template <class T>
 void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector<int32_t>& bounds,
-                     const std::vector<int32_t>& aux, int ctas_per_sm, cudaStream_t s) {
+                     const std::vector<int32_t>& aux, int ctas_per_sm, int side, cudaStream_t s) {
   if ((int32_t)M.host_rp.size() != M.nrows + 1) throw Error(GPDHG_ERR_INTERNAL, "matrix has no host row pointer");
   const int K = (int)bounds.size() - 1;
   std::vector<Tile> tiles;
@@ -107,8 +180,9 @@ void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector
     inst_cta[k] = (int32_t)cta_inst.size();
     inst_split[k] = splits;
     const size_t t0 = tiles.size();
-    list_tiles(M.host_rp.data(), bounds[k], bounds[k + 1], k, aux.empty() ? 0 : aux[k], TileTraits<T>::kNnz,
-               TileTraits<T>::kEMax, tiles, splits, carries);
+    const TileConfig cfg = choose_tile_config<T>(M.host_rp.data(), bounds[k], bounds[k + 1], side);
+    list_tiles(M.host_rp.data(), bounds[k], bounds[k + 1], k, aux.empty() ? 0 : aux[k], cfg.tile_nnz,
+               cfg.e_floor, tiles, splits, carries);
     // warp-streamed rows first, in row order, then the other tiles in row order: CTAs then
     // hold one kind of work (a power-law A' scatters thousands of such rows among short ones)
     std::stable_partition(tiles.begin() + t0, tiles.end(), [](const Tile& t) { return t.e_log2 == kWarpLong; });
@@ -118,7 +192,7 @@ void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector
     // CTAs one wave, up to kTilesPerCtaMax
     const long long nt = (long long)(tiles.size() - t0);
     const long long slots = 152LL * ctas_per_sm;
-    const long long tpc = std::min<long long>(kTilesPerCtaMax, std::max<long long>(kTilesPerCtaMin, (nt + slots - 1) / slots));
+    const long long tpc = std::min<long long>(cfg.tpc_max, std::max<long long>(kTilesPerCtaMin, (nt + slots - 1) / slots));
     long long open = 0;   // tiles in the CTA being filled
     int open_code = 0;    // its tiles' kind: 0 normal, kWarpLong, else the group code
     for (size_t q = t0; q < tiles.size(); ++q) {
@@ -181,8 +255,8 @@ void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector
 }
 
 template void build_tile_plan<float>(TilePlan<float>&, const DeviceMatrix&, const std::vector<int32_t>&,
-                                     const std::vector<int32_t>&, int, cudaStream_t);
+                                     const std::vector<int32_t>&, int, int, cudaStream_t);
 template void build_tile_plan<double>(TilePlan<double>&, const DeviceMatrix&, const std::vector<int32_t>&,
-                                      const std::vector<int32_t>&, int, cudaStream_t);
+                                      const std::vector<int32_t>&, int, int, cudaStream_t);
 
 }  // namespace gpdhg

@@ -104,6 +104,33 @@ struct TilePlan {
   }
 };
 
+// Plan parameters of one instance's tiles. The kernels take any values within the limits
+// below; choose_tile_config picks them per instance from its row-length histogram.
+struct TileConfig {
+  int32_t tile_nnz;   // nonzeros per warp tile at most (<= 32 * kEMax); longer rows up to
+                      // kWarpShare are warp-streamed
+  int32_t e_floor;    // a lane's run is at least min(ceil(nnz / rows), e_floor) nonzeros (about
+                      // one row per lane when rows are short; 1 turns the rule off)
+  int32_t tpc_max;    // tiles per CTA at most (kTilesPerCtaMin..kTilesPerCtaMax)
+};
+constexpr int kTileSideAt = 0;   // the primal kernel's plan (rows of A')
+constexpr int kTileSideA = 1;    // the dual kernel's plan (rows of A)
+// Row-length histogram of an instance: the share of its nonzeros in rows of length
+// [2^b, 2^(b+1)) for b = 0..kHistBins-2 (the last bin takes longer rows), then
+// log2(nonzeros) / 32 as a size feature.
+constexpr int kHistBins = 16;
+constexpr int kHistLen = kHistBins + 1;
+void row_histogram(const int32_t* rp, int32_t r0, int32_t r1, float* h);
+template <class T>
+TileConfig default_tile_config();
+// The measured table's entry nearest (L1 distance over the histogram) to the instance's,
+// for the plan's precision and side; the default when the table has none. A process-wide
+// override (set_tile_override, used by the tuning sweep) takes precedence.
+template <class T>
+TileConfig choose_tile_config(const int32_t* rp, int32_t r0, int32_t r1, int side);
+// precision: GPDHG_PRECISION_FP64 or GPDHG_PRECISION_FP32; cfg NULL clears the override.
+void set_tile_override(int precision, int side, const TileConfig* cfg);
+
 // Appends the tiles of rows [r0, r1) of a CSR with row pointer rp (instance inst). An empty
 // range still gets one empty tile (the instance's step decision runs in its CTA).
 void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t aux, int tile_nnz, int e_max,
@@ -114,6 +141,6 @@ void list_tiles(const int32_t* rp, int32_t r0, int32_t r1, int32_t inst, int32_t
 // (M.view<T>() must hold them).
 template <class T>
 void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector<int32_t>& bounds,
-                     const std::vector<int32_t>& aux, int ctas_per_sm, cudaStream_t s);
+                     const std::vector<int32_t>& aux, int ctas_per_sm, int side, cudaStream_t s);
 
 }  // namespace gpdhg

@@ -211,6 +211,7 @@ SIGNATURES = {
     "gpdhg_batch_destroy": (C.c_int, [C.c_void_p]),
     "gpdhg_convergence_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_double] + [_dp] * 8
                                   + [C.c_double, C.c_double, C.c_void_p, C.POINTER(ConvergenceInformation)]),
+    "gpdhg_set_tile_override": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "gpdhg_server_footprint": (C.c_double, [C.POINTER(LpDesc), C.POINTER(Params)]),
     "gpdhg_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
     "gpdhg_server_submit": (C.c_int, [C.c_void_p, C.POINTER(LpDesc), C.POINTER(Params),

@@ -402,6 +402,21 @@ gpdhg_status gpdhg_convergence_noalloc(int32_t num_variables, int32_t num_constr
                                        gpdhg_convergence_information* out);
 
 /* ---------------------------------------------------------------------------------
+ * Tile-plan tuning hook. No counterpart in the reference.
+ *
+ * The step kernels' work plan (warp tiles, lane runs, tiles per CTA) takes its parameters
+ * from a table measured on GB300 and keyed by the row-length histogram of each instance's
+ * matrix. The sweep that measures the table (cupdlp.jl_gb300/tune_tiles.py) pins the
+ * parameters with this process-wide override for plans built afterwards: precision
+ * GPDHG_PRECISION_FP64 or GPDHG_PRECISION_FP32, side 0 for the primal kernel's plan (rows of
+ * A') and 1 for the dual kernel's (rows of A); tile_nnz = 0 removes the override. Values are
+ * clamped to what the kernels take (tile_nnz 32..32 x the lane run limit, e_floor 1..the
+ * lane run limit, tpc_max 8..96). Results depend on the plan only through summation order.
+ * ------------------------------------------------------------------------------- */
+gpdhg_status gpdhg_set_tile_override(int32_t precision, int32_t side, int32_t tile_nnz, int32_t e_floor,
+                                     int32_t tpc_max);
+
+/* ---------------------------------------------------------------------------------
  * Serving loop: continuous batching of arriving LPs (no reference counterpart: a request
  * loop around optimize(), src/primal_dual_hybrid_gradient_gpu.jl:457).
  *
