@@ -87,10 +87,14 @@ TileConfig choose_tile_config(const int32_t* rp, int32_t r0, int32_t r1, int sid
   }
   float h[kHistLen];
   row_histogram(rp, r0, r1, h);
+  // the table was measured on lone solves of large matrices; smaller instances (latency
+  // bound alone, and run side by side with others in a batch, where the lone optimum did not
+  // carry over) keep the default parameters
+  if (h[kHistBins] < kTileTableMinSize) return default_tile_config<T>();
   const TileTableEntry* best = nullptr;
   double best_d = 0.0;
   for (const TileTableEntry& e : kTileTable) {
-    if (e.fp64 != (q == 0) || e.side != side) continue;
+    if (e.fp64 != (q == 0) || e.side != side || e.hist[kHistBins] < kTileTableMinSize) continue;
     double d = 0.0;
     for (int b = 0; b < kHistLen; ++b) d += std::fabs((double)e.hist[b] - (double)h[b]);
     if (!best || d < best_d) {

@@ -121,11 +121,14 @@ constexpr int kTileSideA = 1;    // the dual kernel's plan (rows of A)
 constexpr int kHistBins = 16;
 constexpr int kHistLen = kHistBins + 1;
 void row_histogram(const int32_t* rp, int32_t r0, int32_t r1, float* h);
+// Instances (and table entries) with fewer than 2^20 nonzeros use the default parameters.
+constexpr float kTileTableMinSize = 20.0f / 32.0f;
 template <class T>
 TileConfig default_tile_config();
 // The measured table's entry nearest (L1 distance over the histogram) to the instance's,
-// for the plan's precision and side; the default when the table has none. A process-wide
-// override (set_tile_override, used by the tuning sweep) takes precedence.
+// for the plan's precision and side, among entries of at least 2^20 nonzeros; the default for
+// smaller instances or when the table has none. A process-wide override (set_tile_override,
+// used by the tuning sweep) takes precedence.
 template <class T>
 TileConfig choose_tile_config(const int32_t* rp, int32_t r0, int32_t r1, int side);
 // precision: GPDHG_PRECISION_FP64 or GPDHG_PRECISION_FP32; cfg NULL clears the override.

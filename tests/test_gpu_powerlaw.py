@@ -70,12 +70,17 @@ def test_reduced_power_law_fp32_refine_reaches_1e4(entry):
           f"{abs(k['primal_objective'] - entry['highs_objective']) / abs(entry['highs_objective']):.2e}")
 
 
-def _reported_equals_recomputed(p, out, rtol):
+def _reported_equals_recomputed(p, out, rtol, rtol_residual=None):
+    """The reported statistics against numpy on the returned iterate. The primal residuals
+    use the average's A x, which the solver keeps as a weighted sum of every step's A x (the
+    reference's sum_primal_product); in FP32 that sum carries FP32 rounding of ~300 steps, so
+    residuals get their own tolerance there."""
     ci = out.iteration_stats[-1].convergence_information[0]
     ref = convergence_information(p, out.primal_solution, out.dual_solution, 1e-4, 1e-4)
     for f in ("primal_objective", "dual_objective", "l2_primal_residual", "l2_dual_residual",
               "l_inf_primal_residual", "l2_primal_variable", "l2_dual_variable", "relative_optimality_gap"):
-        assert getattr(ci, f) == pytest.approx(ref[f], rel=rtol, abs=1e-12), (f, getattr(ci, f), ref[f])
+        tol = rtol_residual if (rtol_residual and f in ("l2_primal_residual", "l_inf_primal_residual")) else rtol
+        assert getattr(ci, f) == pytest.approx(ref[f], rel=tol, abs=1e-12), (f, getattr(ci, f), ref[f])
 
 
 @pytest.mark.parametrize("entry", STUDY, ids=lambda e: f"m{e['m']}")
@@ -104,4 +109,7 @@ def test_full_power_law_statistics_are_those_of_the_returned_iterate(full_power_
     assert out.termination_reason == LIMIT
     # FP32 iterates: the statistics are FP64 sums over FP32 vectors, with cancellation in the
     # dual objective's bound terms (~1e12 here), so they agree to FP32 round-off only
-    _reported_equals_recomputed(p, out, rtol=1e-5 if precision == cupdlp.Precision.FP32 else 1e-9)
+    if precision == cupdlp.Precision.FP32:
+        _reported_equals_recomputed(p, out, rtol=1e-5, rtol_residual=1e-4)
+    else:
+        _reported_equals_recomputed(p, out, rtol=1e-9)
