@@ -86,6 +86,90 @@ __global__ void __launch_bounds__(1024) exclusive_scan_kernel(uint32_t* __restri
   }
 }
 
+// Device-wide exclusive scan of len counts in three launches: per-block totals of
+// kScanBlock consecutive counts (coalesced), one CTA scanning the totals in place
+// (exclusive_scan_kernel), then each block scanning its counts from its total's offset.
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanBlock = kScanThreads * kScanItems;
+
+__global__ void __launch_bounds__(kScanThreads) scan_block_totals_kernel(const uint32_t* __restrict__ v, long long len,
+                                                                         uint32_t* __restrict__ totals) {
+  __shared__ uint32_t warp_sum[kScanThreads / 32];
+  const long long base = (long long)blockIdx.x * kScanBlock;
+  uint32_t s = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const long long i = base + j * kScanThreads + threadIdx.x;
+    if (i < len) s += v[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < kScanThreads / 32; ++w) t += warp_sum[w];
+    totals[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_block_apply_kernel(uint32_t* __restrict__ v, long long len,
+                                                                        const uint32_t* __restrict__ offsets) {
+  __shared__ uint32_t sh[kScanBlock];
+  __shared__ uint32_t warp_sum[kScanThreads / 32];
+  const long long base = (long long)blockIdx.x * kScanBlock;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const int q = j * kScanThreads + threadIdx.x;
+    sh[q] = base + q < len ? v[base + q] : 0u;
+  }
+  __syncthreads();
+  // thread t scans its kScanItems consecutive counts
+  uint32_t loc[kScanItems];
+  uint32_t run = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    loc[j] = run;
+    run += sh[threadIdx.x * kScanItems + j];
+  }
+  // exclusive scan of the thread totals: inclusive within the warp, then across warps
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t inc = run;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += u;
+  }
+  if (lane == 31) warp_sum[warp] = inc;
+  __syncthreads();
+  uint32_t before = offsets[blockIdx.x];
+  for (int w = 0; w < warp; ++w) before += warp_sum[w];
+  before += inc - run;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) sh[threadIdx.x * kScanItems + j] = before + loc[j];
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const int q = j * kScanThreads + threadIdx.x;
+    if (base + q < len) v[base + q] = sh[q];
+  }
+}
+
+void exclusive_scan(uint32_t* v, long long len, DBuf<uint32_t>& totals, cudaStream_t s) {
+  const long long blocks = (len + kScanBlock - 1) / kScanBlock;
+  if (blocks <= 1) {
+    exclusive_scan_kernel<<<1, 1024, 0, s>>>(v, len);
+    CK_LAUNCH();
+    return;
+  }
+  if ((long long)totals.n < blocks) totals.alloc((size_t)blocks);
+  scan_block_totals_kernel<<<(unsigned)blocks, kScanThreads, 0, s>>>(v, len, totals.get());
+  CK_LAUNCH();
+  exclusive_scan_kernel<<<1, 1024, 0, s>>>(totals.get(), blocks);
+  CK_LAUNCH();
+  scan_block_apply_kernel<<<(unsigned)blocks, kScanThreads, 0, s>>>(v, len, totals.get());
+  CK_LAUNCH();
+}
+
 __global__ void __launch_bounds__(kSortThreads) digit_scatter_kernel(const uint32_t* __restrict__ keys,
                                                                      const uint32_t* __restrict__ vals, long long len,
                                                                      int shift, const uint32_t* __restrict__ offs,
@@ -163,6 +247,7 @@ void transpose_on_device(const DeviceMatrix& A, DeviceMatrix& At, cudaStream_t s
   DBuf<uint32_t> v0(std::max<long long>(nnz, 1)), v1(std::max<long long>(nnz, 1));
   DBuf<int32_t> rows(std::max<long long>(nnz, 1));
   DBuf<uint32_t> hist;
+  DBuf<uint32_t> scan_totals;
   if (nnz > 0) {
     row_of_kernel<<<grid_of(nnz), 256, 0, s>>>(m, nnz, A.row_ptr.get(), rows.get());
     CK_LAUNCH();
@@ -175,8 +260,7 @@ void transpose_on_device(const DeviceMatrix& A, DeviceMatrix& At, cudaStream_t s
     for (int shift = 0; shift < 32 && n > 1 && ((uint32_t)(n - 1) >> shift) != 0u; shift += 8) {
       digit_hist_kernel<<<tiles, kSortThreads, 0, s>>>(ka, nnz, shift, hist.get(), tiles);
       CK_LAUNCH();
-      exclusive_scan_kernel<<<1, 1024, 0, s>>>(hist.get(), (long long)kDigits * tiles);
-      CK_LAUNCH();
+      exclusive_scan(hist.get(), (long long)kDigits * tiles, scan_totals, s);
       digit_scatter_kernel<<<tiles, kSortThreads, 0, s>>>(ka, va, nnz, shift, hist.get(), tiles, kb, vb);
       CK_LAUNCH();
       std::swap(ka, kb);
