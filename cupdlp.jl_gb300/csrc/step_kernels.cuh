@@ -352,6 +352,18 @@ struct DualIn {
   T sk;
 };
 
+// FP64 dual kernels run the epilogue of their warp tiles' rows after all of the CTA's row
+// sums are in shared memory, one row per thread. Summed tile by tile, a tile's epilogue (about
+// a dozen FP64 instructions per row) runs on only the lanes that own its rows, a handful when
+// rows are longer than a lane's run, yet every warp-wide FP64 instruction occupies GB300's
+// narrow FP64 pipe for the whole warp: on the power-law LP that made the pipe, not memory, the
+// bound (79% busy). FP32 keeps the per-tile epilogue (its pipe is wide, and the shared-memory
+// row buffer would take L1 from the gathers).
+template <class T>
+constexpr bool kDenseEpilogue = sizeof(T) == 8;
+template <class T>
+constexpr int kDenseSlots = kDenseEpilogue<T> ? kTilesPerCtaMax * kTileRows : 1;
+
 template <class T>
 __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualArgs<T> a) {
   __shared__ T rs_all[kBlock / 32][32];
@@ -454,6 +466,60 @@ __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualA
     if (has && sub == 0) load_in(t, E0);
     if (!commit_only) group_row_sum(a.A.col, a.A.val, a.dx, t, has, W, sub, wlane, rs);
     if (has && sub == 0) finish(t, E0);
+  } else if (kDenseEpilogue<T>) {
+    // warp tiles (never split): every row sum into the CTA's slot buffer, then the epilogue
+    // with one row per thread, slot by slot (slot = the row's position among the tiles' rows)
+    __shared__ T csum[kDenseSlots<T>];
+    __shared__ int32_t slot_begin[kTilesPerCtaMax + 1];
+    if (threadIdx.x == 0) {
+      int o = 0;
+      for (int q = 0; q < nt; ++q) {
+        slot_begin[q] = o;
+        o += tl[q].rows;
+      }
+      slot_begin[nt] = o;
+    }
+    __syncthreads();
+    if (!commit_only) {
+      for (int q = warp; q < nt; q += kBlock / 32) {
+        const Tile t = tl[q];
+        tile_load(a.A.row_ptr, a.plan.icol, a.plan.ival, t, L0);
+        tile_sums(a.A.col, a.A.val, a.dx, t, L0, rs);
+        if (lane < t.rows) csum[slot_begin[q] + lane] = rs[lane];
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    const int nslots = slot_begin[nt];
+    for (int sl = threadIdx.x; sl < nslots; sl += kBlock) {
+      int lo = 0, hi = nt - 1;   // the last tile starting at or before the slot (the non-empty one)
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (slot_begin[mid] <= sl) lo = mid;
+        else hi = mid - 1;
+      }
+      const int i = tl[lo].row_begin + (sl - slot_begin[lo]);
+      const T y = lds(ycur + i), kx = lds(kxcur + i);
+      if (commit_only) {
+        sts(a.sy + i, lds(a.sy + i) + y * w);
+        sts(a.skx + i, lds(a.skx + i) + kx * w);
+        continue;
+      }
+      const T bi = lds(a.b + i);
+      if (pending) {
+        sts(a.sy + i, lds(a.sy + i) + y * w);
+        sts(a.skx + i, lds(a.skx + i) + kx * w);
+      }
+      const T rsum = csum[sl];
+      const T kdx = direct ? rsum - kx : rsum;
+      T v = y + od * ((bi - T(2) * kdx) - kx);   // (:247), extrapolation coefficient 1
+      if (i >= tl[lo].aux) v = imax(v, T(0));      // (:254)
+      const T d = v - y;
+      ynew[i] = y + d;                             // y += dy (:306)
+      sts(kxnew + i, direct ? rsum : kx + kdx);    // Kx += K dx (:304)
+      acc_i = fma(kdx, d, acc_i);
+      acc_d = fma(d, d, acc_d);
+    }
   } else {
     for (int q = warp; q < nt; q += kBlock / 32) {
       const Tile t = tl[q];
