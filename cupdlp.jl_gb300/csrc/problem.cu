@@ -598,12 +598,15 @@ void apply_column_order(gpdhg_problem* p) {
     relabel_kernel<<<(unsigned)((p->A.nnz + 255) / 256), 256, 0, s>>>(p->A.nnz, dinv.get(), p->A.col.get());
     CK_LAUNCH();
   }
+  // the permuted n-vectors: all gathers in flight together; the old vectors are freed after
+  // the synchronisation below
+  std::vector<DBuf<double>> old_vectors;
   for (DBuf<double>* v : {&p->l, &p->u, &p->c, &p->ol, &p->ou, &p->oc, &p->var}) {
     DBuf<double> t((size_t)n);
     gather_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, dperm.get(), v->get(), t.get());
     CK_LAUNCH();
     std::swap(*v, t);
-    CK(cudaStreamSynchronize(s));   // t (the old vector) is freed at the end of this scope
+    old_vectors.push_back(std::move(t));
   }
   // A' of the renumbered A (its rows are the columns in the new order, each listing its
   // entries in increasing row as before), then A again from A', so that every row of A lists
