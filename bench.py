@@ -75,6 +75,9 @@ def parse():
                          "workload uses 1000, since neither the reference loop nor this one "
                          "reaches 1e-4 on it within a benchmark's time)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", choices=["fp64", "fp32", "fp32_refine"], default=None,
+                    help="override the workload's precision (profiling one precision's kernels)")
+    ap.add_argument("--no-reference-gpu", action="store_true", help="skip the reference-form GPU baseline")
     return ap.parse_args()
 
 
@@ -592,6 +595,10 @@ def run_ours(args):
     torch.cuda.set_device(local)
     torch.zeros(1, device="cuda")
     lp, prec, desc = workload(args.workload)
+    if args.precision:
+        prec = {"fp64": cupdlp.Precision.FP64, "fp32": cupdlp.Precision.FP32,
+                "fp32_refine": cupdlp.Precision.FP32_REFINE}[args.precision]
+        desc += f" (precision set to {prec.name})"
     iters = args.iters or DEFAULT_ITERS.get(args.workload, 0)
     params = cupdlp.default_parameters(tolerance=args.tolerance, precision=prec, record_iteration_stats=False,
                                        iteration_limit=iters or 2**31 - 1)
@@ -704,7 +711,7 @@ def run_ours(args):
 
     # the reference's loop in its own GPU form, same problem and iteration budget (rank 0)
     rge = None
-    if rank == 0:
+    if rank == 0 and not args.no_reference_gpu:
         try:
             _, rge = reference_gpu_equiv(sq, params)
             our_sec = t_max / args.steps
