@@ -4,7 +4,8 @@ row-length histogram (choose_tile_config in csrc/tiles.cu).
 
 Run on a GB300 from the repository root, then rebuild the library:
 
-    python cupdlp.jl_gb300/tune_tiles.py [--iters 200] [--quick]
+    python cupdlp.jl_gb300/tune_tiles.py [--iters 200] [--quick] [--min-gain 0.03]
+    python cupdlp.jl_gb300/tune_tiles.py --reapply [--min-gain 0.03]   # the rule on the stored times
 
 For each tuning matrix, precision (FP32, FP64) and candidate (tile_nnz, e_floor, tpc_max),
 the parameters are pinned with gpdhg_set_tile_override, a problem handle is built and
@@ -13,7 +14,9 @@ solved for a fixed number of iterations with per-kernel CUDA-event timing
 primal kernel's time depends only on the plan of A' and the dual's only on the plan of A, so
 each side keeps its own best candidate. The table stores, per matrix, precision and side, the
 row-length histogram of that side's matrix and the best parameters; the measured times of
-the default and of the best candidate are kept as comments.
+the default and of the best candidate are kept as comments. A candidate replaces the default
+parameters only where it is faster by at least --min-gain (3%): smaller differences are within
+the run-to-run spread of one measurement and would change a plan for nothing.
 """
 from __future__ import annotations
 
@@ -22,6 +25,7 @@ import ctypes as C
 import itertools
 import math
 import os
+import re
 import sys
 import time
 
@@ -99,7 +103,13 @@ def main():
     ap.add_argument("--iters", type=int, default=200)
     ap.add_argument("--quick", action="store_true", help="leave out the 21M-nonzero power-law LP")
     ap.add_argument("--out", default=TABLE)
+    ap.add_argument("--min-gain", type=float, default=0.03)
+    ap.add_argument("--reapply", action="store_true", help="re-apply --min-gain to the stored table")
     args = ap.parse_args()
+    if args.reapply:
+        entries, iters = read_table(TABLE)
+        write_table(args.out, entries, iters, args.min_gain)
+        return
     lib = _abi.load()
     entries = []
     for name, lp in matrices(args.quick):
@@ -113,27 +123,48 @@ def main():
             for side in (0, 1):
                 best = min(cands, key=lambda c: times[c][side])
                 entries.append(dict(name=name, fp64=precision == "FP64", side=side, hist=hist[side], cfg=best,
-                                    t_best=times[best][side], t_default=times[DEFAULT[precision]][side]))
+                                    best=best, t_best=times[best][side], t_default=times[DEFAULT[precision]][side]))
                 print(f"{name:15s} {precision} side {side}: best {best} {times[best][side] * 1e6:8.1f} us, "
                       f"default {times[DEFAULT[precision]][side] * 1e6:8.1f} us", flush=True)
         print(f"  ({time.time() - t0:.0f} s)", flush=True)
-    write_table(args.out, entries, args.iters)
+    write_table(args.out, entries, args.iters, args.min_gain)
 
 
-def write_table(path, entries, iters):
+def read_table(path):
+    """The entries of a written table, with their measured times (from the comments)."""
+    text = open(path).read()
+    iters = int(re.search(r"over (\d+) iterations", text).group(1))
+    pat = re.compile(r'// (\w+) (FP32|FP64) side (\d): ([\d.]+) us \(default ([\d.]+) us; measured best '
+                     r'\((\d+), (\d+), (\d+)\)\)\n\s*\{"\w+", \w+, \d, \{([^}]*)\}')
+    entries = []
+    for m in pat.finditer(text):
+        best = (int(m.group(6)), int(m.group(7)), int(m.group(8)))
+        entries.append(dict(name=m.group(1), fp64=m.group(2) == "FP64", side=int(m.group(3)),
+                            t_best=float(m.group(4)) * 1e-6, t_default=float(m.group(5)) * 1e-6, best=best,
+                            hist=[float(v.rstrip("f")) for v in m.group(9).split(",")]))
+    return entries, iters
+
+
+def write_table(path, entries, iters, min_gain):
+    for e in entries:
+        prec = "FP64" if e["fp64"] else "FP32"
+        gain = 1.0 - e["t_best"] / e["t_default"] if e["t_default"] > 0 else 0.0
+        e["cfg"] = e["best"] if gain >= min_gain else DEFAULT[prec]
     lines = ['// tile_table.h — measured tile plan parameters by row-length histogram.', '//',
              '// Written by cupdlp.jl_gb300/tune_tiles.py from a sweep of the plan parameters on one',
              '// GB300: for each tuning matrix, precision and kernel side, the histogram of its rows',
              '// (row_histogram) and the parameters with the lowest measured kernel time. The planner',
              '// takes the entry nearest to an instance\'s histogram (choose_tile_config).',
-             f'// Kernel times: microseconds per launch over {iters} iterations, best vs default parameters.',
+             f'// Kernel times: microseconds per launch over {iters} iterations, best vs default parameters;',
+             f'// the best replaces the default where it is at least {100 * min_gain:.0f}% faster.',
              '#pragma once', '', '#include <cstdint>', '', 'namespace gpdhg {', '',
              'struct TileTableEntry {', '  const char* name;', '  bool fp64;', '  int side;', '  float hist[17];',
              '  int32_t tile_nnz, e_floor, tpc_max;', '};', '', 'inline constexpr TileTableEntry kTileTable[] = {']
     for e in entries:
         h = ", ".join(f"{v:.4f}f" for v in e["hist"])
         lines.append(f'    // {e["name"]} {"FP64" if e["fp64"] else "FP32"} side {e["side"]}: '
-                     f'{e["t_best"] * 1e6:.1f} us (default {e["t_default"] * 1e6:.1f} us)')
+                     f'{e["t_best"] * 1e6:.1f} us (default {e["t_default"] * 1e6:.1f} us; measured best '
+                     f'({e["best"][0]}, {e["best"][1]}, {e["best"][2]}))')
         lines.append(f'    {{"{e["name"]}", {"true" if e["fp64"] else "false"}, {e["side"]}, {{{h}}}, '
                      f'{e["cfg"][0]}, {e["cfg"][1]}, {e["cfg"][2]}}},')
     lines += ['};', '', '}  // namespace gpdhg', '']
