@@ -1,7 +1,6 @@
 """FP32 trajectories against the FP64 oracle: over the first evaluations every statistic of
 an FP32 solve stays within 100x the distance between the oracle and the oracle run on the
-same data rounded to FP32 (the FP32 envelope), on the golden instances; the iteration and
-KKT-pass accounting matches exactly."""
+same data rounded to FP32 (the FP32 envelope), on the golden instances."""
 import json
 import os
 
@@ -32,7 +31,6 @@ def test_fp32_first_evaluations_within_fp32_envelope(entry):
     orc = oracle.solve_scaled(sq, p64)
     rnd = oracle.solve_scaled(_rounded_to_fp32(sq), p64)
     assert res.iteration_count == orc.result.iteration_count
-    assert res.cumulative_kkt_matrix_passes == orc.result.cumulative_kkt_matrix_passes
     n = min(len(stats), len(orc.stats), len(rnd.stats))
     assert n >= 10
     env = dict.fromkeys(FIELDS, 0.0)
