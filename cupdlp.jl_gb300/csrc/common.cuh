@@ -4,12 +4,30 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <stdexcept>
 #include <string>
 
 #include "gpdhg.h"
 
 namespace gpdhg {
+
+// Phase timing of problem creation and solve set-up, printed to stderr when the environment
+// variable GPDHG_TRACE is set (a diagnostic; nothing else reads it).
+struct PhaseTrace {
+  bool on;
+  std::chrono::steady_clock::time_point t;
+  PhaseTrace() : on(std::getenv("GPDHG_TRACE") != nullptr), t(std::chrono::steady_clock::now()) {}
+  void mark(const char* what) {
+    if (!on) return;
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "gpdhg trace: %-28s %8.2f ms\n", what,
+                 std::chrono::duration<double, std::milli>(now - t).count());
+    t = now;
+  }
+};
 
 // A failure that maps onto one gpdhg_status at the ABI boundary.
 struct Error : std::runtime_error {

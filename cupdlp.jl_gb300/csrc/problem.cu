@@ -347,12 +347,18 @@ void narrow_indices(const int64_t* src, int64_t len, int64_t base, std::vector<i
 }  // namespace
 
 void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d) {
+  PhaseTrace tr;
   validate_lp_desc(d, true);
+  tr.mark("validate");
   init_with(p, d, d->values, d->nnz, 0.0, [&](cudaStream_t s) {
     upload_csr(p->A, d->num_constraints, d->num_variables, d->row_ptr, d->col_idx, d->values, s);
+    tr.mark("upload A");
     transpose_on_device(p->A, p->At, s);
+    tr.mark("transpose");
   });
+  tr.mark("vectors, schedules, scalars");
   apply_column_order(p);
+  tr.mark("column order");
 }
 
 namespace {
@@ -583,11 +589,13 @@ __global__ void gather_kernel(int32_t n, const int32_t* __restrict__ perm, const
 }  // namespace
 
 void apply_column_order(gpdhg_problem* p) {
+  PhaseTrace tr;
   const int32_t n = p->n;
   std::vector<int32_t> degree((size_t)n);
   for (int32_t j = 0; j < n; ++j) degree[(size_t)j] = p->At.host_rp[(size_t)j + 1] - p->At.host_rp[(size_t)j];
   std::vector<int32_t> perm;
   if (!choose_column_order(degree, perm)) return;
+  tr.mark("  order: choose");
   cudaStream_t s = p->stream;
   std::vector<int32_t> inv((size_t)n);
   for (int32_t k = 0; k < n; ++k) inv[(size_t)perm[(size_t)k]] = k;
@@ -612,9 +620,12 @@ void apply_column_order(gpdhg_problem* p) {
   // entries in increasing row as before), then A again from A', so that every row of A lists
   // its entries in increasing new column (the layout a caller's own sorted CSR of the
   // renumbered LP gives, ties in their previous order)
+  tr.mark("  order: relabel, gathers");
   transpose_on_device(p->A, p->At, s);
   transpose_on_device(p->At, p->A, s);
+  tr.mark("  order: two transposes");
   set_row_items(p->At, s);
+  tr.mark("  order: row items");
   // the 2-norms over the columns are summed in the new order (an LP whose caller already
   // sorted its columns gets the same scalars, bit for bit)
   std::vector<double> hc((size_t)n), hoc((size_t)n);
@@ -624,6 +635,7 @@ void apply_column_order(gpdhg_problem* p) {
   p->norm2_c_scaled = norm2(hc.data(), n);
   p->l2_c = norm2(hoc.data(), n);
   p->col_perm.swap(perm);
+  tr.mark("  order: norms");
 }
 
 void ensure_fp32_values(gpdhg_problem* p) {

@@ -138,6 +138,7 @@ struct Workspace {
   DBuf<double> part_p_split, part_d_split;
 
   explicit Workspace(gpdhg_problem* p) : P(p), n(p->n), m(p->m), st_host(1), red_host(64) {
+    PhaseTrace tr;
     const size_t N = std::max(n, 1), M = std::max(m, 1);
     cudaStream_t s = P->stream;
     if constexpr (sizeof(T) == sizeof(double)) {
@@ -183,6 +184,7 @@ struct Workspace {
     }
     plan_thread.join();
     if (plan_err) std::rethrow_exception(plan_err);
+    tr.mark(sizeof(T) == 8 ? "FP64 vectors and plans" : "FP32 vectors and plans");
     part_p.alloc(plan_p.num_ctas);
     part_d.alloc(2 * (size_t)plan_d.num_ctas);
     part_p_split.alloc(std::max(plan_p.num_splits, 1));
@@ -208,7 +210,9 @@ struct Workspace {
     }
     CK(cudaEventCreate(&ev0));
     CK(cudaEventCreate(&ev1));
+    tr.mark("segments, partials");
     build_graphs();
+    tr.mark("step graphs");
   }
   ~Workspace() {
     for (cudaGraphExec_t g : graphs)
