@@ -234,6 +234,42 @@ int grid_of(long long len) { return (int)std::max<long long>(1, std::min<long lo
 
 }  // namespace
 
+namespace {
+// key[j] = max_key - (rp[j + 1] - rp[j]): ascending keys = decreasing row lengths
+__global__ void length_key_kernel(int32_t n, const int32_t* __restrict__ rp, uint32_t max_key,
+                                  uint32_t* __restrict__ key) {
+  const int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) key[j] = max_key - (uint32_t)(rp[j + 1] - rp[j]);
+}
+}  // namespace
+
+void order_rows_by_length(const DeviceMatrix& M, std::vector<int32_t>& order, cudaStream_t s) {
+  const int32_t n = M.nrows;
+  order.assign((size_t)n, 0);
+  if (n == 0) return;
+  uint32_t max_len = 0;
+  for (int32_t j = 0; j < n; ++j) max_len = std::max<uint32_t>(max_len, (uint32_t)(M.host_rp[j + 1] - M.host_rp[j]));
+  DBuf<uint32_t> k0((size_t)n), k1((size_t)n), v0((size_t)n), v1((size_t)n), hist, scan_totals;
+  length_key_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, M.row_ptr.get(), max_len, k0.get());
+  CK_LAUNCH();
+  iota_kernel<<<grid_of(n), 256, 0, s>>>(n, v0.get());
+  CK_LAUNCH();
+  const int tiles = (int)((n + kSortTile - 1) / kSortTile);
+  hist.alloc((size_t)kDigits * tiles);
+  uint32_t *ka = k0.get(), *kb = k1.get(), *va = v0.get(), *vb = v1.get();
+  for (int shift = 0; shift < 32 && (max_len >> shift) != 0u; shift += 8) {
+    digit_hist_kernel<<<tiles, kSortThreads, 0, s>>>(ka, n, shift, hist.get(), tiles);
+    CK_LAUNCH();
+    exclusive_scan(hist.get(), (long long)kDigits * tiles, scan_totals, s);
+    digit_scatter_kernel<<<tiles, kSortThreads, 0, s>>>(ka, va, n, shift, hist.get(), tiles, kb, vb);
+    CK_LAUNCH();
+    std::swap(ka, kb);
+    std::swap(va, vb);
+  }
+  CK(cudaMemcpyAsync(order.data(), va, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+}
+
 void transpose_on_device(const DeviceMatrix& A, DeviceMatrix& At, cudaStream_t s) {
   const int32_t m = A.nrows, n = A.ncols;
   const long long nnz = A.nnz;

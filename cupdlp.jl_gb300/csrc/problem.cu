@@ -357,7 +357,8 @@ void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d) {
     tr.mark("transpose");
   });
   tr.mark("vectors, schedules, scalars");
-  apply_column_order(p);
+  apply_column_order(p, d->objective_vector,
+                     d->original_objective_vector ? d->original_objective_vector : d->objective_vector);
   tr.mark("column order");
 }
 
@@ -412,7 +413,8 @@ void problem_init_csc(gpdhg_problem* p, const gpdhg_lp_desc* d, const int64_t* c
     upload_csr(p->At, n, m, rp.data(), ri.data(), nz_val, s);
     transpose_on_device(p->At, p->A, s);
   });
-  apply_column_order(p);
+  apply_column_order(p, d->objective_vector,
+                     d->original_objective_vector ? d->original_objective_vector : d->objective_vector);
 }
 
 void problem_init_two_sided(gpdhg_problem* p, const gpdhg_two_sided_desc* t, const int64_t* col_ptr,
@@ -538,7 +540,7 @@ void problem_init_two_sided(gpdhg_problem* p, const gpdhg_two_sided_desc* t, con
     transpose_on_device(At, p->A, s);
     if (!identity) transpose_on_device(p->A, At, s);
   });
-  apply_column_order(p);
+  apply_column_order(p, nullptr, nullptr);
 }
 
 bool choose_column_order(const std::vector<int32_t>& degree, std::vector<int32_t>& perm) {
@@ -588,15 +590,26 @@ __global__ void gather_kernel(int32_t n, const int32_t* __restrict__ perm, const
 }
 }  // namespace
 
-void apply_column_order(gpdhg_problem* p) {
+void apply_column_order(gpdhg_problem* p, const double* c_host, const double* oc_host) {
   PhaseTrace tr;
   const int32_t n = p->n;
-  std::vector<int32_t> degree((size_t)n);
-  for (int32_t j = 0; j < n; ++j) degree[(size_t)j] = p->At.host_rp[(size_t)j + 1] - p->At.host_rp[(size_t)j];
-  std::vector<int32_t> perm;
-  if (!choose_column_order(degree, perm)) return;
-  tr.mark("  order: choose");
+  const long long total = p->At.host_rp[(size_t)n];
+  if (n < kColumnOrderMinColumns || total == 0) return;
+  // the rule needs the top 1% of columns to hold kColumnOrderTopShare of the nonzeros, which
+  // the longest column alone decides against when top x its length falls short
+  int32_t dmax = 0;
+  for (int32_t j = 0; j < n; ++j) dmax = std::max(dmax, p->At.host_rp[(size_t)j + 1] - p->At.host_rp[(size_t)j]);
+  const int32_t top = std::max<int32_t>(1, (n + 99) / 100);
+  if ((double)dmax * (double)top < kColumnOrderTopShare * (double)total) return;
   cudaStream_t s = p->stream;
+  // the order of choose_column_order (decreasing degree, ties by index), sorted on the device
+  std::vector<int32_t> perm;
+  order_rows_by_length(p->At, perm, s);
+  long long top_nnz = 0;
+  for (int32_t k = 0; k < top; ++k)
+    top_nnz += p->At.host_rp[(size_t)perm[(size_t)k] + 1] - p->At.host_rp[(size_t)perm[(size_t)k]];
+  if ((double)top_nnz < kColumnOrderTopShare * (double)total) return;
+  tr.mark("  order: choose");
   std::vector<int32_t> inv((size_t)n);
   for (int32_t k = 0; k < n; ++k) inv[(size_t)perm[(size_t)k]] = k;
   DBuf<int32_t> dperm((size_t)n), dinv((size_t)n);
@@ -627,10 +640,18 @@ void apply_column_order(gpdhg_problem* p) {
   set_row_items(p->At, s);
   tr.mark("  order: row items");
   // the 2-norms over the columns are summed in the new order (an LP whose caller already
-  // sorted its columns gets the same scalars, bit for bit)
+  // sorted its columns gets the same scalars, bit for bit), from the caller's arrays when
+  // they are at hand, else from the permuted device vectors
   std::vector<double> hc((size_t)n), hoc((size_t)n);
-  CK(cudaMemcpyAsync(hc.data(), p->c.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(hoc.data(), p->oc.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (c_host && oc_host) {
+    for (int32_t k = 0; k < n; ++k) {
+      hc[(size_t)k] = c_host[perm[(size_t)k]];
+      hoc[(size_t)k] = oc_host[perm[(size_t)k]];
+    }
+  } else {
+    CK(cudaMemcpyAsync(hc.data(), p->c.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(hoc.data(), p->oc.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  }
   CK(cudaStreamSynchronize(s));
   p->norm2_c_scaled = norm2(hc.data(), n);
   p->l2_c = norm2(hoc.data(), n);
