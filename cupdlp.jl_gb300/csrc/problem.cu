@@ -357,8 +357,7 @@ void problem_init(gpdhg_problem* p, const gpdhg_lp_desc* d) {
     tr.mark("transpose");
   });
   tr.mark("vectors, schedules, scalars");
-  apply_column_order(p, d->objective_vector,
-                     d->original_objective_vector ? d->original_objective_vector : d->objective_vector);
+  apply_column_order(p);
   tr.mark("column order");
 }
 
@@ -413,8 +412,7 @@ void problem_init_csc(gpdhg_problem* p, const gpdhg_lp_desc* d, const int64_t* c
     upload_csr(p->At, n, m, rp.data(), ri.data(), nz_val, s);
     transpose_on_device(p->At, p->A, s);
   });
-  apply_column_order(p, d->objective_vector,
-                     d->original_objective_vector ? d->original_objective_vector : d->objective_vector);
+  apply_column_order(p);
 }
 
 void problem_init_two_sided(gpdhg_problem* p, const gpdhg_two_sided_desc* t, const int64_t* col_ptr,
@@ -540,7 +538,7 @@ void problem_init_two_sided(gpdhg_problem* p, const gpdhg_two_sided_desc* t, con
     transpose_on_device(At, p->A, s);
     if (!identity) transpose_on_device(p->A, At, s);
   });
-  apply_column_order(p, nullptr, nullptr);
+  apply_column_order(p);
 }
 
 bool choose_column_order(const std::vector<int32_t>& degree, std::vector<int32_t>& perm) {
@@ -590,7 +588,7 @@ __global__ void gather_kernel(int32_t n, const int32_t* __restrict__ perm, const
 }
 }  // namespace
 
-void apply_column_order(gpdhg_problem* p, const double* c_host, const double* oc_host) {
+void apply_column_order(gpdhg_problem* p) {
   PhaseTrace tr;
   const int32_t n = p->n;
   const long long total = p->At.host_rp[(size_t)n];
@@ -640,18 +638,11 @@ void apply_column_order(gpdhg_problem* p, const double* c_host, const double* oc
   set_row_items(p->At, s);
   tr.mark("  order: row items");
   // the 2-norms over the columns are summed in the new order (an LP whose caller already
-  // sorted its columns gets the same scalars, bit for bit), from the caller's arrays when
-  // they are at hand, else from the permuted device vectors
+  // sorted its columns gets the same scalars, bit for bit), from the permuted device vectors
+  // (a copy back is faster than gathering the caller's arrays on the host)
   std::vector<double> hc((size_t)n), hoc((size_t)n);
-  if (c_host && oc_host) {
-    for (int32_t k = 0; k < n; ++k) {
-      hc[(size_t)k] = c_host[perm[(size_t)k]];
-      hoc[(size_t)k] = oc_host[perm[(size_t)k]];
-    }
-  } else {
-    CK(cudaMemcpyAsync(hc.data(), p->c.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(hoc.data(), p->oc.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-  }
+  CK(cudaMemcpyAsync(hc.data(), p->c.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(hoc.data(), p->oc.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   p->norm2_c_scaled = norm2(hc.data(), n);
   p->l2_c = norm2(hoc.data(), n);

@@ -173,9 +173,8 @@ constexpr double kColumnOrderTopShare = 0.2;
 bool choose_column_order(const std::vector<int32_t>& degree, std::vector<int32_t>& perm);
 // Renumbers the columns of a built problem by choose_column_order's rule (the order sorted on
 // the device; A's column indices, each row of A re-sorted by its new column, A' rebuilt,
-// every n-vector permuted on the device) and records the order in col_perm. c_host / oc_host:
-// the caller's scaled and original objective vectors (for the column norms), or NULL.
-void apply_column_order(gpdhg_problem* p, const double* c_host, const double* oc_host);
+// every n-vector permuted on the device) and records the order in col_perm.
+void apply_column_order(gpdhg_problem* p);
 // The rows of M in decreasing length, ties in row order (a stable radix sort on the device).
 void order_rows_by_length(const DeviceMatrix& M, std::vector<int32_t>& order, cudaStream_t s);
 // v (n entries, handle order) rewritten in the caller's column order, in place.
