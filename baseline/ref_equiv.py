@@ -2,7 +2,7 @@
 (cuSPARSE CSR_ALG2, per-kernel synchronisation, host-side reductions, FP64): the
 "reference on the same GPU" baseline that the benchmark measures beside the library.
 
-BASELINE ONLY: used by bench.py and its tests, never by the `cupdlp` package.
+Used by bench.py and its tests only, never by the `cupdlp` package.
 """
 from __future__ import annotations
 
