@@ -148,6 +148,19 @@ struct PrimalIn {
   T u;
 };
 
+// FP64 step kernels run row epilogues after the CTA's row sums are in shared memory, one row
+// per thread (the dual kernel for its warp tiles, the primal kernel for its warp-streamed
+// rows). Summed tile by tile, a tile's epilogue (about a dozen FP64 instructions per row) runs
+// on only the lanes that own its rows (a handful when rows are longer than a lane's run, one
+// for a streamed row), yet every warp-wide FP64 instruction occupies GB300's narrow FP64 pipe
+// for the whole warp: on the power-law LP that made the pipe, not memory, the dual's bound
+// (79% busy). FP32 keeps the per-tile epilogue (its pipe is wide, and the shared-memory row
+// buffer would take L1 from the gathers).
+template <class T>
+constexpr bool kDenseEpilogue = sizeof(T) == 8;
+template <class T>
+constexpr int kDenseSlots = kDenseEpilogue<T> ? kTilesPerCtaMax * kTileRows : 1;
+
 template <class T>
 __global__ void __launch_bounds__(kBlock, kPrimalCtasPerSm<T>) primal_step_kernel(PrimalArgs<T> a) {
   __shared__ T rs_all[kBlock / 32][32];
@@ -244,6 +257,42 @@ __global__ void __launch_bounds__(kBlock, kPrimalCtasPerSm<T>) primal_step_kerne
     if (has && sub == 0) load_in(t, E0);
     if (pending) group_row_sum(a.At.col, a.At.val, yg, t, has, W, sub, wlane, rs);
     if (has && sub == 0) finish(t, E0);
+  } else if (kDenseEpilogue<T> && nt > 0 && tl[0].e_log2 == kWarpLong) {
+    // FP64 CTAs of warp-streamed rows (one row per tile): the warps stream their rows' sums
+    // into shared memory, then thread q runs the epilogue of tile q's row, so the FP64
+    // instructions of the epilogue run on full warps instead of on each warp's lane 0
+    __shared__ T lsum[kDenseEpilogue<T> ? kTilesPerCtaMax : 1];
+    if (pending)
+      for (int q = warp; q < nt; q += kBlock / 32) {
+        const T sum = long_row_sum(a.At.col, a.At.val, yg, tl[q]);
+        if (lane == 0) lsum[q] = sum;
+      }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nt; q += kBlock) {
+      const Tile& t = tl[q];
+      const int j = t.row_begin;
+      PrimalIn<T> e{};
+      if (!commit_only) {
+        e.c = lds(a.c + j);
+        e.l = lds(a.l + j);
+        e.u = lds(a.u + j);
+      }
+      if (pending) {
+        e.dx = lds(a.dx + j);
+        if (!direct) e.x = lds(a.x + j);
+        e.sx = lds(a.sx + j);
+        const T ktyv = lsum[q];
+        const T xv = direct ? e.dx : e.x + e.dx;   // x += dx (:303)
+        sts(a.x + j, xv);
+        sts(a.kty + j, ktyv);                       // K'y = A'y (:307)
+        sts(a.sx + j, e.sx + xv * w);               // weighted sum (src/saddle_point_gpu.jl:137)
+        if (!commit_only) candidate(j, xv, ktyv, e, t, false);
+      } else {
+        e.x = lds(a.x + j);
+        e.dx = lds(a.kty + j);
+        candidate(j, e.x, e.dx, e, t, false);
+      }
+    }
   } else {
     // each warp walks its tiles q = warp, warp + 8, ...: a tile's epilogue inputs, row
     // offsets, columns and values are all issued before any of them is used
@@ -351,18 +400,6 @@ struct DualIn {
   T sy;
   T sk;
 };
-
-// FP64 dual kernels run the epilogue of their warp tiles' rows after all of the CTA's row
-// sums are in shared memory, one row per thread. Summed tile by tile, a tile's epilogue (about
-// a dozen FP64 instructions per row) runs on only the lanes that own its rows, a handful when
-// rows are longer than a lane's run, yet every warp-wide FP64 instruction occupies GB300's
-// narrow FP64 pipe for the whole warp: on the power-law LP that made the pipe, not memory, the
-// bound (79% busy). FP32 keeps the per-tile epilogue (its pipe is wide, and the shared-memory
-// row buffer would take L1 from the gathers).
-template <class T>
-constexpr bool kDenseEpilogue = sizeof(T) == 8;
-template <class T>
-constexpr int kDenseSlots = kDenseEpilogue<T> ? kTilesPerCtaMax * kTileRows : 1;
 
 template <class T>
 __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualArgs<T> a) {
