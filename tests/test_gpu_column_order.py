@@ -8,6 +8,7 @@ reference's (oracle, rtol 1e-9 over 10 iterations, iterates included), a batch i
 equals its lone solve, and warm starts, current iterates and device rescaling vectors come
 back in the caller's order."""
 import numpy as np
+import scipy.sparse as sp
 import pytest
 
 import cupdlp
@@ -101,3 +102,32 @@ def test_warm_start_current_iterate_and_rescaling_in_caller_order(skewed):
         con, var = du.rescaling()
     np.testing.assert_allclose(con, sq.constraint_rescaling, rtol=1e-14, atol=0)
     np.testing.assert_allclose(var, sq.variable_rescaling, rtol=1e-14, atol=0)
+
+
+def test_every_entry_orders_the_columns_alike(skewed):
+    """The CSR, CSC and two-sided entries of the same skewed LP build the same renumbered
+    handle: the same solve, bit for bit (rescaled on the GPU for the unscaled entries)."""
+    from cupdlp.solver import unscaled_desc
+    from cupdlp.types import TwoSidedQpProblem
+    p = skewed.problem
+    params = cupdlp.default_parameters(tolerance=1e-12, iteration_limit=100, time_sec_limit=60.0)
+    with DeviceProblem.from_unscaled(p, params) as dp:
+        r, x, y = dp.solve(params)
+    a = sp.csc_matrix(p.constraint_matrix)
+    a.sort_indices()
+    with DeviceProblem.from_csc(unscaled_desc(p), a, index_base=1, unscaled_params=params) as dq:
+        r2, x2, y2 = dq.solve(params)
+    assert r2.total_number_iterations == r.total_number_iterations
+    assert np.array_equal(x2, x) and np.array_equal(y2, y)
+    # the same LP as an MPS reader returns it: '=' rows with equal bounds, '>=' rows open above
+    m, neq = p.num_constraints, p.num_equalities
+    hi = p.right_hand_side.copy()
+    hi[neq:] = np.inf
+    t = TwoSidedQpProblem(p.variable_lower_bound.copy(), p.variable_upper_bound.copy(), p.right_hand_side.copy(),
+                          hi, a, p.objective_constant, p.objective_vector.copy())
+    with DeviceProblem.from_two_sided(t, index_base=0, unscaled_params=params) as dt:
+        nv, neq2, ns, order = dt.standard_form()
+        r3, x3, y3 = dt.solve(params)
+    assert (nv, neq2, ns) == (p.num_variables, neq, 0) and np.array_equal(order, np.arange(m))
+    assert r3.total_number_iterations == r.total_number_iterations
+    assert np.array_equal(x3, x) and np.array_equal(y3, y)
