@@ -6,7 +6,10 @@
 // the HBM budget, resident request count, cohort size), after lingering briefly for more.
 // The cohort is packed into one segmented batch and solved; every instance retires from the
 // device work the moment it terminates, and its result is handed out at that moment (a
-// small request does not wait for the large ones it was packed with). The cohort's memory
+// small request does not wait for the large ones it was packed with). Once at most a quarter
+// of a cohort's instances still run, the cohort gives up its worker slot: another worker (the
+// server keeps twice `workers` threads) may start a new cohort beside its stragglers, so
+// arriving requests back-fill the device while the stragglers finish. The cohort's memory
 // returns to the budget when its last instance is done: the packed buffers are freed
 // together. Cohorts of different workers run concurrently, so a request that arrives while
 // others are on the GPU starts as soon as a worker and memory are free and its kernels
@@ -116,7 +119,8 @@ class Server {
     if (cfg_.workers <= 0) cfg_.workers = 2;
     if (cfg_.linger_sec < 0.0) cfg_.linger_sec = 0.0;
     else if (cfg_.linger_sec == 0.0) cfg_.linger_sec = 0.002;
-    for (int w = 0; w < cfg_.workers; ++w) workers_.emplace_back([this] { worker_main(); });
+    // twice the cohort slots in threads: a straggling cohort's slot goes to a new cohort
+    for (int w = 0; w < 2 * cfg_.workers; ++w) workers_.emplace_back([this] { worker_main(); });
   }
 
   ~Server() {
@@ -202,6 +206,9 @@ class Server {
     return cohort;
   }
 
+  // A cohort slot is free: fewer cohorts hold one than `workers` (stragglers hold none).
+  bool slot_free() const { return active_cohorts_ - straggling_cohorts_ < cfg_.workers; }
+
   void worker_main() {
     cudaSetDevice(device_);
     while (true) {
@@ -209,33 +216,40 @@ class Server {
       double fp = 0.0;
       {
         std::unique_lock<std::mutex> lk(mu_);
-        cv_work_.wait(lk, [&] { return stop_ || !queue_.empty(); });
+        cv_work_.wait(lk, [&] { return stop_ || (!queue_.empty() && slot_free()); });
         if (stop_) return;
         if ((int)queue_.size() < cfg_.max_cohort && cfg_.linger_sec > 0.0)
           cv_work_.wait_for(lk, std::chrono::duration<double>(cfg_.linger_sec),
                             [&] { return stop_ || (int)queue_.size() >= cfg_.max_cohort; });
         if (stop_) return;
+        if (!slot_free()) continue;
         cohort = pick_cohort(fp);
         if (cohort.empty()) {
           // the head waits for memory held by running cohorts (their end notifies)
           if (!queue_.empty() && resident_ > 0) cv_work_.wait(lk);
           continue;
         }
+        ++active_cohorts_;
       }
-      if (batch_takes(cohort.front()->params)) solve(cohort);
+      bool straggling = false;
+      if (batch_takes(cohort.front()->params)) solve(cohort, straggling);
       else solve_alone(cohort);
       {
         std::lock_guard<std::mutex> lk(mu_);
         in_use_ -= fp;
         resident_ -= (int)cohort.size();
         for (auto& r : cohort) r->done = true;
+        --active_cohorts_;
+        if (straggling) --straggling_cohorts_;
       }
       cv_done_.notify_all();
       cv_work_.notify_all();
     }
   }
 
-  void solve(std::vector<std::shared_ptr<Request>>& cohort) {
+  // `straggling` is set (under the lock, with straggling_cohorts_) when at most a quarter of
+  // the cohort's instances are still running.
+  void solve(std::vector<std::shared_ptr<Request>>& cohort, bool& straggling) {
     const int k = (int)cohort.size();
     std::vector<gpdhg_lp_desc> descs(k);
     std::vector<gpdhg_result> results(k);
@@ -252,15 +266,24 @@ class Server {
     std::string error;
     gpdhg_batch* b = nullptr;
     // an instance's result is handed out as soon as it has terminated
+    int running = k;
     const std::function<void(int)> retire = [&](int q) {
+      bool freed_slot = false;
       {
         std::lock_guard<std::mutex> lk(mu_);
         Request& r = *cohort[q];
         r.status = GPDHG_OK;
         r.result = results[q];
         r.done = true;
+        --running;
+        if (!straggling && k > 1 && 4 * running <= k && running > 0) {
+          straggling = true;
+          ++straggling_cohorts_;
+          freed_slot = true;
+        }
       }
       cv_done_.notify_all();
+      if (freed_slot) cv_work_.notify_all();
     };
     try {
       b = new gpdhg_batch();
@@ -336,6 +359,8 @@ class Server {
   std::map<uint64_t, std::shared_ptr<Request>> all_;  // submitted and not collected
   double in_use_ = 0.0;
   int resident_ = 0;
+  int active_cohorts_ = 0;       // cohorts being solved
+  int straggling_cohorts_ = 0;   // of those, the ones that gave up their slot
   uint64_t next_ticket_ = 1;
   bool stop_ = false;
   std::vector<std::thread> workers_;

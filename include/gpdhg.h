@@ -430,7 +430,9 @@ gpdhg_status gpdhg_set_tile_override(int32_t precision, int32_t side, int32_t ti
  * are free, and their kernels overlap with the running cohorts' on the device. An instance
  * that terminates stops launching work at once and its result can be collected at that
  * moment; its cohort's memory is released when the cohort's last instance terminates.
- * Requests whose parameters a batch does not take (FP32_REFINE with its FP64 hand-off, the
+ * Once at most a quarter of a cohort's instances still run, the cohort no longer counts
+ * against `workers`: a new cohort of waiting requests starts beside its stragglers (the
+ * server keeps 2 x workers threads for this). Requests whose parameters a batch does not take (FP32_REFINE with its FP64 hand-off, the
  * constant step size) are solved one after another as lone problems by the worker that picks
  * them. Each result is bit-identical to solving the same LP alone with the same parameters
  * (a batch gives every instance the same arithmetic as a lone solve). Zero config fields
@@ -442,7 +444,7 @@ typedef struct gpdhg_server_config {
   double hbm_budget_bytes;   /* admission budget for resident requests [half the free device memory] */
   int32_t max_resident;      /* requests resident on the device at once, all cohorts [4096] */
   int32_t max_cohort;        /* requests packed into one device batch [256] */
-  int32_t workers;           /* cohorts advanced concurrently [2] */
+  int32_t workers;           /* cohorts advanced concurrently, stragglers not counted [2] */
   int32_t reserved_int;
   double linger_sec;         /* a free worker waits this long for more requests [0.002] */
   double reserved[2];

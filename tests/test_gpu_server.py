@@ -127,3 +127,27 @@ def test_results_are_handed_out_as_each_instance_terminates():
     for k, sq in enumerate(small):
         _same(got_small[k], _alone(sq, params), k)
     _same(got_big, _alone(big, params), "big")
+
+
+def test_a_straggling_cohort_gives_its_slot_to_new_requests():
+    """One worker slot; a cohort of one slow LP and three quick ones. Once the quick three have
+    retired, the cohort is a straggler and no longer holds the slot: a request submitted then
+    is packed into a new cohort and answered while the slow LP is still on the device."""
+    big = cupdlp.rescale_problem(10, False, 1.0, 0, synthetic.power_law_lp(1, m=300, n=600,
+                                                                          target_nnz=3000).problem)
+    small = [cupdlp.rescale_problem(10, False, 1.0, 0, synthetic.known_optimum_lp(40 + k, m=60, n=120,
+                                                                                  density=0.05).problem)
+             for k in range(4)]
+    params = cupdlp.default_parameters(tolerance=1e-8, precision=cupdlp.Precision.FP64,
+                                       iteration_limit=400_000, time_sec_limit=300.0)
+    with Server(workers=1, max_cohort=4, linger_sec=0.05) as srv:
+        tickets = [srv.submit(scaled_desc(sq), params) for sq in [big] + small[:3]]
+        for t in tickets[1:]:
+            srv.wait(t, timeout=600.0)
+        late = srv.submit(scaled_desc(small[3]), params)
+        got_late = srv.wait(late, timeout=600.0)
+        big_pending = srv.poll(tickets[0]) is None
+        got_big = srv.wait(tickets[0], timeout=600.0)
+    assert big_pending
+    assert got_big[0].iteration_count > got_late[0].iteration_count
+    _same(got_late, _alone(small[3], params), "late")
