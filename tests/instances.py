@@ -78,6 +78,26 @@ def long_rows_lp(seed=31, m=45000, n=45000, per_column=2, lengths=LONG_ROW_LENGT
     return synthetic._planted(rng, a, int(round(0.6 * m)), np.full(n, 10.0), f"long_rows_m{m}_n{n}_s{seed}")
 
 
+def ragged_rows_lp(seed=61, m=4000, n=3000):
+    """A planted-optimum LP (bounds [0, 10]) whose warp tiles mix every row shape inside one
+    warp's run: a quarter of the rows empty, a quarter with one nonzero, a quarter with 2-6 and
+    a quarter with 10-80; a fifth of the columns empty and the rest drawn with skewed
+    popularity, so that A' (the primal kernel's rows) is as ragged. Values N(0,1)."""
+    from cupdlp import synthetic
+    rng = np.random.default_rng(seed)
+    kind = rng.integers(0, 4, m)
+    lens = np.where(kind == 0, 0, np.where(kind == 1, 1, np.where(kind == 2, rng.integers(2, 7, m),
+                                                                   rng.integers(10, 81, m))))
+    w = 1.0 / np.arange(1, n + 1) ** 1.5
+    w[rng.permutation(n)[: n // 5]] = 0.0
+    w /= w.sum()
+    rows = np.repeat(np.arange(m), lens)
+    cols = np.concatenate([rng.choice(n, size=k, replace=False, p=w) for k in lens if k > 0])
+    a = sp.csc_matrix((rng.standard_normal(rows.size), (rows, cols)), shape=(m, n))
+    a.sort_indices()
+    return synthetic._planted(rng, a, int(round(0.6 * m)), np.full(n, 10.0), f"ragged_rows_m{m}_n{n}_s{seed}")
+
+
 def infeasible_planted_lp(kind, seed=51, m=400, n=800, density=0.01):
     """A planted-optimum LP made infeasible: kind "primal" repeats equality row 0 with its
     right-hand side raised by 1 (two contradictory equalities); kind "dual" appends a column
