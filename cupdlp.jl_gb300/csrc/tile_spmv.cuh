@@ -15,28 +15,63 @@ struct TileLoad {
   T v[TileTraits<T>::kEMax];
 };
 
+// One 128-bit load of a lane: a group of 4 columns, 4 FP32 values or 2 FP64 values.
+__device__ __forceinline__ void load_group(const int32_t* p, int32_t* d) {
+  const int4 w = lds(reinterpret_cast<const int4*>(p));
+  d[0] = w.x;
+  d[1] = w.y;
+  d[2] = w.z;
+  d[3] = w.w;
+}
+__device__ __forceinline__ void load_group(const float* p, float* d) {
+  const float4 w = lds(reinterpret_cast<const float4*>(p));
+  d[0] = w.x;
+  d[1] = w.y;
+  d[2] = w.z;
+  d[3] = w.w;
+}
+__device__ __forceinline__ void load_group(const double* p, double* d) {
+  const double2 w = lds(reinterpret_cast<const double2*>(p));
+  d[0] = w.x;
+  d[1] = w.y;
+}
+
+// The lane's E elements (E = 2^e_log2) of one interleaved array (interleaved_slot): 128-bit
+// group loads when E fills a group of G = 16 / sizeof(U), else one element per load; all are
+// issued before any is used. Padding slots are loaded with the run (they exist).
+template <class U, int kEMax>
+__device__ __forceinline__ void load_run(const U* __restrict__ base, int data_begin, int e_log2, U* d) {
+  constexpr int G = 16 / (int)sizeof(U);
+  const int lane = threadIdx.x & 31;
+  const int E = 1 << e_log2;
+  if (E >= G) {
+    const U* p = base + data_begin + G * lane;
+#pragma unroll
+    for (int g = 0; g < kEMax / G; ++g) {
+      if (g * G >= E) break;  // uniform over the warp
+      load_group(p + 32 * G * g, d + G * g);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < (G - 1 < kEMax ? G - 1 : kEMax); ++j) {
+      if (j >= E) break;  // E is the same for the whole warp: a uniform exit
+      d[j] = lds(base + data_begin + 32 * j + lane);
+    }
+  }
+}
+
 // Issues the loads of tile t (none is used here, so all are in flight together). The lane's
-// j-th column and value come from the plan's lane-interleaved copy (slot data_begin + 32 j +
-// lane), so each load instruction of the warp is one coalesced access; slots past the tile's
-// nonzeros are not read.
+// columns and values come from the plan's lane-interleaved copy (interleaved_slot), so each
+// load instruction of the warp is one coalesced access; padding slots are loaded with the
+// lane's run but never gathered.
 template <class T>
 __device__ __forceinline__ void tile_load(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ icol,
                                           const T* __restrict__ ival, const Tile& t, TileLoad<T>& L) {
   if (t.e_log2 < 0) return;  // a long row: streamed by long_row_sum / group_row_sum
   const int lane = threadIdx.x & 31;
-  const int E = 1 << t.e_log2;
-  const int kb = lane << t.e_log2;
-  const int ke = min(t.nnz, kb + E);
   L.rpl = lane <= t.rows ? row_ptr[t.row_begin + lane] : 0;
-  const int32_t* cp = icol + t.data_begin + lane;
-  const T* vp = ival + t.data_begin + lane;
-#pragma unroll
-  for (int j = 0; j < TileTraits<T>::kEMax; ++j) {
-    if (j >= E) break;  // E is the same for the whole warp: a uniform exit, nothing issued past it
-    const bool in = kb + j < ke;
-    L.c[j] = in ? lds(cp + 32 * j) : 0;
-    L.v[j] = in ? lds(vp + 32 * j) : T(0);
-  }
+  load_run<int32_t, TileTraits<T>::kEMax>(icol, t.data_begin, t.e_log2, L.c);
+  load_run<T, TileTraits<T>::kEMax>(ival, t.data_begin, t.e_log2, L.v);
 }
 
 // A warp's rounds r0, r0 + step, ... (< nnz) of a long row: 32 x kLongRound coalesced

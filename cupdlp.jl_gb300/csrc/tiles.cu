@@ -16,7 +16,8 @@ int ceil_log2(long long v) {
 }
 
 // One warp per warp tile: lane l's j-th nonzero (CSR position nnz_begin + l E + j) goes to
-// slot data_begin + 32 j + l; slots past the tile's nonzeros get column 0 and value 0.
+// its interleaved_slot in the column and the value copy; slots past the tile's nonzeros get
+// column 0 and value 0.
 template <class T>
 __global__ void __launch_bounds__(256) interleave_tiles_kernel(const Tile* __restrict__ tiles, int ntiles,
                                                               const int32_t* __restrict__ col,
@@ -29,10 +30,9 @@ __global__ void __launch_bounds__(256) interleave_tiles_kernel(const Tile* __res
   const int E = 1 << t.e_log2;
   for (int j = 0; j < E; ++j) {
     const int k = lane * E + j;
-    const long long dst = (long long)t.data_begin + 32LL * j + lane;
     const bool in = k < t.nnz;
-    icol[dst] = in ? col[(long long)t.nnz_begin + k] : 0;
-    ival[dst] = in ? val[(long long)t.nnz_begin + k] : T(0);
+    icol[interleaved_slot(t.data_begin, t.e_log2, lane, j, 4)] = in ? col[(long long)t.nnz_begin + k] : 0;
+    ival[interleaved_slot(t.data_begin, t.e_log2, lane, j, (int)sizeof(T))] = in ? val[(long long)t.nnz_begin + k] : T(0);
   }
 }
 }  // namespace

@@ -16,11 +16,14 @@
 // Lane-interleaved copy: lane l of a warp tile owns the tile's nonzeros [l E, (l + 1) E)
 // (consecutive, so that rows are summed with one FMA per nonzero and few shuffles). Read
 // from the CSR, the j-th load of every lane would hit 32 addresses E elements apart. The plan
-// therefore keeps a copy of every warp tile's columns and values with the lane's j-th nonzero
-// at data_begin + 32 j + l: each of a lane's E loads is one coalesced 128-byte (FP32) or
-// 256-byte (FP64) access of the warp. Slots past the tile's nonzeros hold column 0 and value 0
-// and are never read. Long rows (warp-streamed, group and split) already stream the CSR
-// coalesced and have no copy.
+// therefore keeps a copy of every warp tile's columns and values in which the lane's nonzeros
+// come in 16-byte groups of G = 16 / (element size) (4 columns or FP32 values, 2 FP64 values):
+// the lane's j-th element sits at data_begin + 32 G (j / G) + G l + j % G (interleaved_slot), so
+// that each group is one 128-bit load of the lane and each such load of the warp is one
+// coalesced 512-byte access. Tiles with E < G keep one element per load (slot data_begin +
+// 32 j + l). Slots past the tile's nonzeros hold column 0 and value 0 and are loaded with the
+// lane's run but never gathered. Long rows (warp-streamed, group and split) already stream the
+// CSR coalesced and have no copy.
 #pragma once
 
 #include <vector>
@@ -48,6 +51,14 @@ constexpr int kTilesPerCtaMax = 96;  // up to twelve per warp for large ones
 template <class T>
 constexpr int kPrimalCtasPerSm = sizeof(T) == 8 ? 4 : 4;
 constexpr int kDualCtasPerSm = 4;
+
+// Slot of lane `lane`'s j-th element in a warp tile's interleaved copy of `bytes`-byte
+// elements (E = 2^e_log2 per lane): 16-byte groups when E fills one.
+__host__ __device__ constexpr long long interleaved_slot(int data_begin, int e_log2, int lane, int j, int bytes) {
+  return (16 / bytes <= (1 << e_log2))
+             ? (long long)data_begin + 32LL * (16 / bytes) * (j / (16 / bytes)) + (16 / bytes) * lane + j % (16 / bytes)
+             : (long long)data_begin + 32LL * j + lane;
+}
 
 constexpr int kWarpLong = -1;  // Tile::e_log2 of a row streamed by one warp
 // Tile::e_log2 of a row summed by 2^g warps (g = 1, 2, 3)
