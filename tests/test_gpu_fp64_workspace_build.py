@@ -1,0 +1,67 @@
+"""GPU tests of the FP64 workspace of an FP32_REFINE solve, built on a helper thread while the
+FP32 phase runs: the result is the same, bit for bit, whichever way the FP64 workspace came
+to exist, a pending build is taken over by a later FP64 solve, and a handle whose build is
+still pending can be destroyed."""
+import numpy as np
+import pytest
+
+import cupdlp
+from cupdlp import synthetic
+from cupdlp.solver import DeviceProblem, scaled_desc
+
+pytestmark = pytest.mark.gpu
+
+
+def _scaled(seed=21):
+    p = synthetic.known_optimum_lp(seed, m=800, n=1600, density=0.01).problem
+    return cupdlp.rescale_problem(10, False, 1.0, 0, p)
+
+
+def _params(precision, tol):
+    return cupdlp.default_parameters(tolerance=tol, precision=precision, iteration_limit=60_000,
+                                     time_sec_limit=300.0)
+
+
+def _same(a, b):
+    (ra, xa, ya), (rb, xb, yb) = a, b
+    assert ra.termination_reason == rb.termination_reason
+    assert ra.iteration_count == rb.iteration_count
+    assert ra.fp64_handoff_iteration == rb.fp64_handoff_iteration
+    assert np.array_equal(xa, xb) and np.array_equal(ya, yb)
+
+
+def test_refine_result_does_not_depend_on_how_the_fp64_workspace_was_built():
+    d = scaled_desc(_scaled())
+    refine = _params(cupdlp.Precision.FP32_REFINE, 1e-8)
+    with DeviceProblem(d) as dp:
+        fresh = dp.solve(refine)              # FP64 workspace built beside the FP32 phase
+    with DeviceProblem(d) as dp:
+        dp.solve(_params(cupdlp.Precision.FP64, 1e-4))   # FP64 workspace built up front
+        warm = dp.solve(refine)
+        again = dp.solve(refine)              # both workspaces cached
+    assert fresh[0].fp64_handoff_iteration > 0
+    _same(fresh, warm)
+    _same(fresh, again)
+
+
+def test_pending_build_is_taken_by_a_later_fp64_solve():
+    d = scaled_desc(_scaled(22))
+    p64 = _params(cupdlp.Precision.FP64, 1e-6)
+    with DeviceProblem(d) as dp:
+        early = dp.solve(_params(cupdlp.Precision.FP32_REFINE, 1e-3))   # ends in the FP32 phase
+        assert early[0].fp64_handoff_iteration < 0
+        after = dp.solve(p64)
+    with DeviceProblem(d) as dp:
+        alone = dp.solve(p64)
+    _same(after, alone)
+
+
+def test_handle_destroyed_while_its_build_is_pending():
+    d = scaled_desc(_scaled(23))
+    for _ in range(3):
+        with DeviceProblem(d) as dp:
+            r, _, _ = dp.solve(_params(cupdlp.Precision.FP32_REFINE, 1e-2))
+            assert r.fp64_handoff_iteration < 0
+    with DeviceProblem(d) as dp:
+        r, _, _ = dp.solve(_params(cupdlp.Precision.FP64, 1e-6))
+    assert r.termination_reason == cupdlp.TerminationReason.TERMINATION_REASON_OPTIMAL
