@@ -401,6 +401,11 @@ struct DualIn {
   T sk;
 };
 
+// The dual kernel's FP64 tiles stop their segmented scan at the longest lane span of a
+// crossing row (tile_sums); FP32 adds are cheap and keep the full scan.
+template <class T>
+constexpr bool kSpanScan = sizeof(T) == 8;
+
 template <class T>
 __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualArgs<T> a) {
   __shared__ T rs_all[kBlock / 32][32];
@@ -521,7 +526,7 @@ __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualA
       for (int q = warp; q < nt; q += kBlock / 32) {
         const Tile t = tl[q];
         tile_load(a.A.row_ptr, a.plan.icol, a.plan.ival, t, L0);
-        tile_sums(a.A.col, a.A.val, a.dx, t, L0, rs);
+        tile_sums<T, kSpanScan<T>>(a.A.col, a.A.val, a.dx, t, L0, rs);
         if (lane < t.rows) csum[slot_begin[q] + lane] = rs[lane];
         __syncwarp();
       }
@@ -563,7 +568,7 @@ __global__ void __launch_bounds__(kBlock, kDualCtasPerSm) dual_step_kernel(DualA
       load_in(t, E0);
       if (!commit_only) {
         tile_load(a.A.row_ptr, a.plan.icol, a.plan.ival, t, L0);
-        tile_sums(a.A.col, a.A.val, a.dx, t, L0, rs);
+        tile_sums<T, kSpanScan<T>>(a.A.col, a.A.val, a.dx, t, L0, rs);
       }
       finish(t, E0);
     }
