@@ -10,7 +10,6 @@
 
 #include <cuda_runtime.h>
 
-#include <future>
 #include <memory>
 #include <vector>
 
@@ -118,9 +117,6 @@ struct gpdhg_problem {
   cudaStream_t stream = nullptr;
   std::unique_ptr<gpdhg::Workspace<double>, gpdhg::WorkspaceDeleter> ws64;
   std::unique_ptr<gpdhg::Workspace<float>, gpdhg::WorkspaceDeleter> ws32;
-  // an FP64 workspace being built on a helper thread while an FP32_REFINE solve runs its FP32
-  // phase (taken into ws64 where it is first needed, or when the handle is destroyed)
-  std::future<gpdhg::Workspace<double>*> ws64_building;
   std::vector<gpdhg_iteration_stats> history;
   std::vector<double> warm_x, warm_y;   // scaled warm start (empty: zero start)
   int last_precision = -1;              // workspace holding the last current iterate

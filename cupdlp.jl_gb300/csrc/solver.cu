@@ -19,7 +19,6 @@
 #include <memory>
 #include <mutex>
 #include <exception>
-#include <future>
 #include <thread>
 #include <limits>
 #include <random>
@@ -138,14 +137,10 @@ struct Workspace {
   TilePlan<T> plan_p, plan_d;
   DBuf<double> part_p_split, part_d_split;
 
-  // Built on `build` (the problem's stream when null): every copy, kernel and graph capture of
-  // the construction goes there and has completed at return; the solve loop then runs on the
-  // problem's stream.
-  explicit Workspace(gpdhg_problem* p, cudaStream_t build = nullptr)
-      : P(p), n(p->n), m(p->m), st_host(1), red_host(64) {
+  explicit Workspace(gpdhg_problem* p) : P(p), n(p->n), m(p->m), st_host(1), red_host(64) {
     PhaseTrace tr;
     const size_t N = std::max(n, 1), M = std::max(m, 1);
-    cudaStream_t s = build ? build : P->stream;
+    cudaStream_t s = P->stream;
     if constexpr (sizeof(T) == sizeof(double)) {
       l = (const T*)P->l.get();
       u = (const T*)P->u.get();
@@ -216,8 +211,7 @@ struct Workspace {
     CK(cudaEventCreate(&ev0));
     CK(cudaEventCreate(&ev1));
     tr.mark("segments, partials");
-    build_graphs(s);
-    CK(cudaStreamSynchronize(s));
+    build_graphs();
     tr.mark("step graphs");
   }
   ~Workspace() {
@@ -251,7 +245,8 @@ struct Workspace {
     P->launches += 2;
   }
 
-  cudaGraphExec_t capture(int pairs, cudaStream_t s) {
+  cudaGraphExec_t capture(int pairs) {
+    cudaStream_t s = P->stream;
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < pairs; ++k) {
@@ -266,8 +261,8 @@ struct Workspace {
     cudaGraphDestroy(g);
     return ex;
   }
-  void build_graphs(cudaStream_t s) {
-    for (int lv = 0; lv < kGraphLevels; ++lv) graphs[lv] = capture(1 << lv, s);
+  void build_graphs() {
+    for (int lv = 0; lv < kGraphLevels; ++lv) graphs[lv] = capture(1 << lv);
   }
   // The same pairs launched directly with an event between every two kernels, for
   // per-kernel CUDA-event timing (events recorded as graph nodes cannot be timed).
@@ -340,12 +335,6 @@ void gpdhg::WorkspaceDeleter::operator()(Workspace<double>* w) const { delete w;
 void gpdhg::WorkspaceDeleter::operator()(Workspace<float>* w) const { delete w; }
 
 gpdhg_problem::~gpdhg_problem() {
-  if (ws64_building.valid()) {
-    try {
-      ws64.reset(ws64_building.get());
-    } catch (...) {
-    }
-  }
   ws64.reset();
   ws32.reset();
   if (stream) cudaStreamDestroy(stream);
@@ -756,61 +745,25 @@ void handoff_to_fp64(gpdhg_problem* P, Workspace<float>& F, Workspace<double>& D
 
 }  // namespace
 
-namespace {
-
-// Starts building the FP64 workspace on a helper thread and a stream of its own (an
-// FP32_REFINE solve needs it at the hand-off; its ~10 ms of host plans, copies and graph
-// captures then overlap the FP32 phase).
-void start_fp64_workspace(gpdhg_problem* P) {
-  if (P->ws64 || P->ws64_building.valid()) return;
-  int device = 0;
-  CK(cudaGetDevice(&device));
-  P->ws64_building = std::async(std::launch::async, [P, device]() -> Workspace<double>* {
-    CK(cudaSetDevice(device));   // a new host thread starts on device 0
-    cudaStream_t bs = nullptr;
-    CK(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
-    Workspace<double>* w = nullptr;
-    try {
-      w = new Workspace<double>(P, bs);
-    } catch (...) {
-      cudaStreamSynchronize(bs);
-      cudaStreamDestroy(bs);
-      throw;
-    }
-    cudaStreamDestroy(bs);
-    return w;
-  });
-}
-
-// The FP64 workspace, from the helper thread's build when one is pending (its error, if it
-// failed, is thrown here), else built now.
-Workspace<double>& fp64_workspace(gpdhg_problem* P) {
-  if (P->ws64_building.valid()) P->ws64.reset(P->ws64_building.get());
-  if (!P->ws64) P->ws64.reset(new Workspace<double>(P));
-  return *P->ws64;
-}
-
-}  // namespace
-
 void solve(gpdhg_problem* P, const gpdhg_params& prm, gpdhg_result* res, double* primal_out, double* dual_out) {
   P->history.clear();
   LoopState L;
   L.launches_at_start = P->launches;
   const int prec = prm.precision;
   if (prec == GPDHG_PRECISION_FP64) {
-    fp64_workspace(P);
+    if (!P->ws64) P->ws64.reset(new Workspace<double>(P));
     L.precision = GPDHG_PRECISION_FP64;
     init_state(P, *P->ws64, prm, L);
     run_phase(P, *P->ws64, prm, L, res, primal_out, dual_out, false);
     return;
   }
-  const bool refine = prec == GPDHG_PRECISION_FP32_REFINE;
-  if (refine) start_fp64_workspace(P);
   if (!P->ws32) P->ws32.reset(new Workspace<float>(P));
   L.precision = GPDHG_PRECISION_FP32;
   init_state(P, *P->ws32, prm, L);
+  const bool refine = prec == GPDHG_PRECISION_FP32_REFINE;
   if (run_phase(P, *P->ws32, prm, L, res, primal_out, dual_out, refine)) return;
-  handoff_to_fp64(P, *P->ws32, fp64_workspace(P));
+  if (!P->ws64) P->ws64.reset(new Workspace<double>(P));
+  handoff_to_fp64(P, *P->ws32, *P->ws64);
   L.precision = GPDHG_PRECISION_FP64;
   L.handoff_iteration = (int)(L.iteration - 1);
   run_phase(P, *P->ws64, prm, L, res, primal_out, dual_out, false);

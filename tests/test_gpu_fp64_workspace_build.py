@@ -1,7 +1,7 @@
-"""GPU tests of the FP64 workspace of an FP32_REFINE solve, built on a helper thread while the
-FP32 phase runs: the result is the same, bit for bit, whichever way the FP64 workspace came
-to exist, a pending build is taken over by a later FP64 solve, and a handle whose build is
-still pending can be destroyed."""
+"""GPU tests of the FP64 workspace of a handle used for several precisions: an FP32_REFINE
+solve gives the same result, bit for bit, whether its FP64 workspace existed before the solve
+or was built at the hand-off, and an FP64 solve after an FP32_REFINE solve that ended in its
+FP32 phase equals the FP64 solve of a fresh handle."""
 import numpy as np
 import pytest
 
@@ -30,11 +30,11 @@ def _same(a, b):
     assert np.array_equal(xa, xb) and np.array_equal(ya, yb)
 
 
-def test_refine_result_does_not_depend_on_how_the_fp64_workspace_was_built():
+def test_refine_result_does_not_depend_on_when_the_fp64_workspace_was_built():
     d = scaled_desc(_scaled())
     refine = _params(cupdlp.Precision.FP32_REFINE, 1e-8)
     with DeviceProblem(d) as dp:
-        fresh = dp.solve(refine)              # FP64 workspace built beside the FP32 phase
+        fresh = dp.solve(refine)              # FP64 workspace built at the hand-off
     with DeviceProblem(d) as dp:
         dp.solve(_params(cupdlp.Precision.FP64, 1e-4))   # FP64 workspace built up front
         warm = dp.solve(refine)
@@ -44,7 +44,7 @@ def test_refine_result_does_not_depend_on_how_the_fp64_workspace_was_built():
     _same(fresh, again)
 
 
-def test_pending_build_is_taken_by_a_later_fp64_solve():
+def test_fp64_solve_after_a_refine_solve_that_ended_in_fp32():
     d = scaled_desc(_scaled(22))
     p64 = _params(cupdlp.Precision.FP64, 1e-6)
     with DeviceProblem(d) as dp:
@@ -54,14 +54,3 @@ def test_pending_build_is_taken_by_a_later_fp64_solve():
     with DeviceProblem(d) as dp:
         alone = dp.solve(p64)
     _same(after, alone)
-
-
-def test_handle_destroyed_while_its_build_is_pending():
-    d = scaled_desc(_scaled(23))
-    for _ in range(3):
-        with DeviceProblem(d) as dp:
-            r, _, _ = dp.solve(_params(cupdlp.Precision.FP32_REFINE, 1e-2))
-            assert r.fp64_handoff_iteration < 0
-    with DeviceProblem(d) as dp:
-        r, _, _ = dp.solve(_params(cupdlp.Precision.FP64, 1e-6))
-    assert r.termination_reason == cupdlp.TerminationReason.TERMINATION_REASON_OPTIMAL
