@@ -80,8 +80,34 @@ void for_each_instance(int count, F f) {
     if (err[k]) std::rethrow_exception(err[k]);
 }
 
+// Allocator of host staging arrays that the instances' threads fill completely: a new element
+// is left as it is (default-initialised) instead of zeroed, which for the packed matrix and
+// vectors of a large batch spares one single-threaded pass over a few GB.
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+  using value_type = T;
+  NoInitAlloc() = default;
+  template <class U>
+  NoInitAlloc(const NoInitAlloc<U>&) noexcept {}
+  template <class U>
+  struct rebind {
+    using other = NoInitAlloc<U>;
+  };
+  template <class U>
+  void construct(U* p) noexcept {
+    ::new ((void*)p) U;
+  }
+  template <class U, class... A>
+  void construct(U* p, A&&... a) {
+    ::new ((void*)p) U(std::forward<A>(a)...);
+  }
+};
+template <class T>
+using HostArray = std::vector<T, NoInitAlloc<T>>;
+
 void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
   if (count <= 0 || !descs) throw Error(GPDHG_ERR_INVALID_ARGUMENT, "batch needs count > 0 and descriptors");
+  PhaseTrace tr;
   B->count = count;
   B->row_off.assign(count + 1, 0);
   B->col_off.assign(count + 1, 0);
@@ -94,6 +120,7 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
   // every descriptor validated (on host threads, one instance each); the error of the first
   // invalid instance is the one reported, as a serial loop would
   for_each_instance(count, [&](int k) { validate_lp_desc(&descs[k], false); });
+  tr.mark("batch: validate");
   long long nnz_total = 0;
   std::vector<long long> nnz_off(count + 1, 0);
   for (int k = 0; k < count; ++k) {
@@ -114,9 +141,10 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
 
   // pack A (block diagonal), the vectors, the per-instance schedules and host scalars: each
   // instance fills its own slices (on host threads); A' is built from A on the GPU
-  std::vector<int32_t> arp(M + 1, 0), acol(nnz_total);
-  std::vector<double> aval(nnz_total);
-  std::vector<double> l(N), u(N), c(N), b(M), ol(N), ou(N), oc(N), ob(M), con(M), var(N);
+  std::vector<int32_t> arp(M + 1, 0);
+  HostArray<int32_t> acol(nnz_total);
+  HostArray<double> aval(nnz_total);
+  HostArray<double> l(N), u(N), c(N), b(M), ol(N), ou(N), oc(N), ob(M), con(M), var(N);
   std::vector<uint8_t> ineq(std::max(M, 1), 0);
   std::vector<std::vector<RowItem>> a_items_of(count);
   for_each_instance(count, [&](int k) {
@@ -158,13 +186,13 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
     for (RowItem it : build_row_items(d.row_ptr, m))
       a_items_of[k].push_back({it.row_begin + ro, it.row_end + ro, it.group, it.mode, it.nnz_begin + (int32_t)z0, it.nnz_count});
     if (m == 0) a_items_of[k].push_back({ro, ro, 1, kItemStaged, (int32_t)z0, 0});  // every instance owns a dual CTA: its decision runs there
-    auto put = [](std::vector<double>& dst, int32_t off, const double* src, const double* fb, int len) {
+    auto put = [](HostArray<double>& dst, int32_t off, const double* src, const double* fb, int len) {
       const double* p = src ? src : fb;
       if (p) std::copy(p, p + len, dst.begin() + off);
       else std::fill(dst.begin() + off, dst.begin() + off + len, 1.0);
     };
     // n-vectors in the instance's column order
-    auto put_n = [&](std::vector<double>& dst, const double* src, const double* fb) {
+    auto put_n = [&](HostArray<double>& dst, const double* src, const double* fb) {
       const double* p = src ? src : fb;
       if (!p) std::fill(dst.begin() + co, dst.begin() + co + n, 1.0);
       else if (perm.empty()) std::copy(p, p + n, dst.begin() + co);
@@ -201,19 +229,20 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
     for (int32_t i = 0; i < m; ++i) { s2 += obb[i] * obb[i]; si = std::max(si, std::fabs(obb[i])); }
     qi.l2_b = std::sqrt(s2); qi.linf_b = si;
   });
+  tr.mark("batch: pack");
   std::vector<RowItem> a_items, t_items;
   for (auto& v : a_items_of) a_items.insert(a_items.end(), v.begin(), v.end());
 
-  auto up_i = [&](DBuf<int32_t>& dst, const std::vector<int32_t>& v) {
+  auto up_i = [&](DBuf<int32_t>& dst, const auto& v) {
     dst.alloc(std::max<size_t>(v.size(), 1));
     if (!v.empty()) CK(cudaMemcpyAsync(dst.get(), v.data(), 4 * v.size(), cudaMemcpyHostToDevice, s));
   };
-  auto up_d = [&](DBuf<double>& dst, const std::vector<double>& v) {
+  auto up_d = [&](DBuf<double>& dst, const auto& v) {
     dst.alloc(std::max<size_t>(v.size(), 1));
     if (!v.empty()) CK(cudaMemcpyAsync(dst.get(), v.data(), 8 * v.size(), cudaMemcpyHostToDevice, s));
   };
   auto up_items = [&](DeviceMatrix& dm, int32_t nrows, int32_t ncols, const std::vector<int32_t>& rp,
-                      const std::vector<int32_t>& col, const std::vector<double>& val, const std::vector<RowItem>& it) {
+                      const HostArray<int32_t>& col, const HostArray<double>& val, const std::vector<RowItem>& it) {
     dm.nrows = nrows;
     dm.ncols = ncols;
     dm.nnz = (long long)col.size();
@@ -226,9 +255,11 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
     if (!it.empty()) CK(cudaMemcpyAsync(dm.items.get(), it.data(), sizeof(RowItem) * it.size(), cudaMemcpyHostToDevice, s));
   };
   up_items(B->A, M, N, arp, acol, aval, a_items);
+  tr.mark("batch: upload A");
   // A' of the packed A on the GPU: the transpose of a block-diagonal matrix is block diagonal
   // with the blocks' transposes in the same order, each the counting sort's (ingest.cu)
   transpose_on_device(B->A, B->At, s);
+  tr.mark("batch: transpose");
   for (int k = 0; k < count; ++k) {
     const int32_t co = B->col_off[k], n = B->col_off[k + 1] - co;
     // the instance's rows of A' from the packed row pointer (absolute nonzero offsets)
@@ -266,6 +297,7 @@ void batch_init(gpdhg_batch* B, int32_t count, const gpdhg_lp_desc* descs) {
   up_i(B->seg_n_begin, bn);
   up_i(B->seg_m_begin, bm);
   CK(cudaStreamSynchronize(s));
+  tr.mark("batch: vectors, schedules");
 }
 
 template <class T>
@@ -308,6 +340,7 @@ struct BatchWorkspace {
   explicit BatchWorkspace(gpdhg_batch* b_) : B(b_), count(b_->count), N(b_->N), M(b_->M),
                                              st_host(b_->count), red_host((size_t)b_->count * 32),
                                              flags_host(4 * (size_t)b_->count) {
+    PhaseTrace tr;
     cudaStream_t s = B->stream;
     if constexpr (sizeof(T) == sizeof(double)) {
       l = (const T*)B->l.get(); u = (const T*)B->u.get(); c = (const T*)B->c.get(); b = (const T*)B->b.get();
@@ -335,10 +368,13 @@ struct BatchWorkspace {
     launch_reciprocal(B->con.get(), rcon.get(), M, s);
     st_dev.alloc(count);
     CK(cudaMemsetAsync(st_dev.get(), 0, sizeof(StepState) * count, s));
+    tr.mark("batch ws: vectors");
     build_tile_plan(plan_p, B->At, B->col_off, {}, kPrimalCtasPerSm<T>, kTileSideAt, s);
+    tr.mark("batch ws: primal plan");
     std::vector<int32_t> ineq_from(count);
     for (int k = 0; k < count; ++k) ineq_from[k] = B->row_off[k] + B->neq[k];
     build_tile_plan(plan_d, B->A, B->row_off, ineq_from, kDualCtasPerSm, kTileSideA, s);
+    tr.mark("batch ws: dual plan");
     part_p.alloc(plan_p.num_ctas);
     part_d.alloc(2 * (size_t)plan_d.num_ctas);
     part_p_split.alloc(std::max(plan_p.num_splits, 1));
@@ -347,6 +383,7 @@ struct BatchWorkspace {
     red_out.alloc((size_t)count * 32);
     flags.alloc(4 * (size_t)count);
     compact(std::vector<char>(count, 0));
+    tr.mark("batch ws: CTA maps, graphs");
   }
   ~BatchWorkspace() {
     for (cudaGraphExec_t g : graphs)

@@ -1,5 +1,8 @@
 // tiles.cu — host builder of the tile plans of the step kernels.
 #include <algorithm>
+#include <atomic>
+#include <exception>
+#include <thread>
 #include <cmath>
 #include <mutex>
 
@@ -43,8 +46,7 @@ void row_histogram(const int32_t* rp, int32_t r0, int32_t r1, float* h) {
   for (int32_t r = r0; r < r1; ++r) {
     const long long len = (long long)rp[r + 1] - rp[r];
     if (len <= 0) continue;
-    int b = 0;
-    while (b < kHistBins - 1 && (2LL << b) <= len) ++b;
+    const int b = std::min(kHistBins - 1, 63 - __builtin_clzll((unsigned long long)len));  // floor(log2 len)
     w[b] += (double)len;
     total += len;
   }
@@ -177,40 +179,97 @@ void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector
                      const std::vector<int32_t>& aux, int ctas_per_sm, int side, cudaStream_t s) {
   if ((int32_t)M.host_rp.size() != M.nrows + 1) throw Error(GPDHG_ERR_INTERNAL, "matrix has no host row pointer");
   const int K = (int)bounds.size() - 1;
-  std::vector<Tile> tiles;
-  std::vector<int32_t> cta_begin, cta_inst, inst_cta(K + 1), inst_split(K + 1);
-  int32_t splits = 0, carries = 0;
-  for (int k = 0; k < K; ++k) {
-    inst_cta[k] = (int32_t)cta_inst.size();
-    inst_split[k] = splits;
-    const size_t t0 = tiles.size();
+  // each instance's tiles and CTAs on their own (on host threads for a batch: the rows of a
+  // packed A' run to tens of millions), then concatenated in instance order with the split
+  // rows and carry slots renumbered after those of the instances before
+  struct Part {
+    std::vector<Tile> tiles;
+    std::vector<int32_t> cta_begin;   // first tile of each CTA, within the instance
+    int32_t splits = 0, carries = 0;
+  };
+  std::vector<Part> parts(K);
+  auto plan_instance = [&](int k) {
+    Part& P = parts[k];
     const TileConfig cfg = choose_tile_config<T>(M.host_rp.data(), bounds[k], bounds[k + 1], side);
     list_tiles(M.host_rp.data(), bounds[k], bounds[k + 1], k, aux.empty() ? 0 : aux[k], cfg.tile_nnz,
-               cfg.e_floor, tiles, splits, carries);
+               cfg.e_floor, P.tiles, P.splits, P.carries);
     // warp-streamed rows first, in row order, then the other tiles in row order: CTAs then
     // hold one kind of work (a power-law A' scatters thousands of such rows among short ones)
-    std::stable_partition(tiles.begin() + t0, tiles.end(), [](const Tile& t) { return t.e_log2 == kWarpLong; });
+    std::stable_partition(P.tiles.begin(), P.tiles.end(), [](const Tile& t) { return t.e_log2 == kWarpLong; });
     // CTAs: 8 / W group tiles of one width W together; warp-streamed rows, and the other
     // tiles, in groups of tpc: 8 while the instance has fewer tiles than one per warp of
     // every resident CTA slot (152 SMs x ctas_per_sm), then as many as make the instance's
     // CTAs one wave, up to kTilesPerCtaMax
-    const long long nt = (long long)(tiles.size() - t0);
+    const long long nt = (long long)P.tiles.size();
     const long long slots = 152LL * ctas_per_sm;
     const long long tpc = std::min<long long>(cfg.tpc_max, std::max<long long>(kTilesPerCtaMin, (nt + slots - 1) / slots));
     long long open = 0;   // tiles in the CTA being filled
     int open_code = 0;    // its tiles' kind: 0 normal, kWarpLong, else the group code
-    for (size_t q = t0; q < tiles.size(); ++q) {
-      const int e = tiles[q].e_log2;
+    for (size_t q = 0; q < P.tiles.size(); ++q) {
+      const int e = P.tiles[q].e_log2;
       const int code = e < 0 ? e : 0;
       const long long cap = code <= group_code(1) ? (8 >> group_log2(code)) : tpc;
       if (open == 0 || code != open_code || open == cap) {
-        cta_begin.push_back((int32_t)q);
-        cta_inst.push_back(k);
+        P.cta_begin.push_back((int32_t)q);
         open = 0;
         open_code = code;
       }
       ++open;
     }
+  };
+  const int threads = std::max(1, std::min<int>(K, (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
+  if (threads == 1) {
+    for (int k = 0; k < K; ++k) plan_instance(k);
+  } else {
+    std::vector<std::exception_ptr> err(K);
+    std::atomic<int> next{0};
+    std::vector<std::thread> th;
+    for (int t = 0; t < threads; ++t)
+      th.emplace_back([&] {
+        for (int k = next++; k < K; k = next++) {
+          try {
+            plan_instance(k);
+          } catch (...) {
+            err[k] = std::current_exception();
+          }
+        }
+      });
+    for (auto& x : th) x.join();
+    for (int k = 0; k < K; ++k)
+      if (err[k]) std::rethrow_exception(err[k]);
+  }
+  std::vector<Tile> tiles;
+  std::vector<int32_t> cta_begin, cta_inst, inst_cta(K + 1), inst_split(K + 1);
+  int32_t splits = 0, carries = 0;
+  {
+    size_t total_tiles = 0, total_ctas = 0;
+    for (const Part& P : parts) {
+      total_tiles += P.tiles.size();
+      total_ctas += P.cta_begin.size();
+    }
+    tiles.reserve(total_tiles);
+    cta_begin.reserve(total_ctas + 1);
+    cta_inst.reserve(total_ctas);
+  }
+  for (int k = 0; k < K; ++k) {
+    Part& P = parts[k];
+    inst_cta[k] = (int32_t)cta_inst.size();
+    inst_split[k] = splits;
+    const int32_t t0 = (int32_t)tiles.size();
+    for (Tile t : P.tiles) {
+      if (t.split >= 0) {
+        t.split += splits;
+        t.carry += carries;
+      }
+      tiles.push_back(t);
+    }
+    for (int32_t b : P.cta_begin) {
+      cta_begin.push_back(t0 + b);
+      cta_inst.push_back(k);
+    }
+    splits += P.splits;
+    carries += P.carries;
+    std::vector<Tile>().swap(P.tiles);
   }
   inst_cta[K] = (int32_t)cta_inst.size();
   inst_split[K] = splits;
