@@ -155,6 +155,7 @@ struct Workspace {
       if (m) launch_convert_d2f(P->b.get(), b_own.get(), m, s);
       l = l_own.get(); u = u_own.get(); c = c_own.get(); b = b_own.get();
     }
+    tr.mark("  ws: FP32 copies");
     // the primal plan (a host pass over the n rows of A') is built on a helper thread while
     // this one allocates the iterate vectors and builds the dual plan
     std::exception_ptr plan_err;
@@ -177,7 +178,9 @@ struct Workspace {
       launch_reciprocal(P->con.get(), rcon.get(), m, s);
       st_dev.alloc(1);
       CK(cudaMemsetAsync(st_dev.get(), 0, sizeof(StepState), s));
+      tr.mark("  ws: iterate buffers");
       build_tile_plan(plan_d, P->A, {0, m}, {P->neq}, kDualCtasPerSm, kTileSideA, s);
+      tr.mark("  ws: dual plan");
     } catch (...) {
       plan_thread.join();
       throw;

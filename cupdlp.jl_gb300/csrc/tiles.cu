@@ -178,6 +178,7 @@ template <class T>
 void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector<int32_t>& bounds,
                      const std::vector<int32_t>& aux, int ctas_per_sm, int side, cudaStream_t s) {
   if ((int32_t)M.host_rp.size() != M.nrows + 1) throw Error(GPDHG_ERR_INTERNAL, "matrix has no host row pointer");
+  PhaseTrace tr;
   const int K = (int)bounds.size() - 1;
   // each instance's tiles and CTAs on their own (on host threads for a batch: the rows of a
   // packed A' run to tens of millions), then concatenated in instance order with the split
@@ -238,6 +239,7 @@ void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector
     for (int k = 0; k < K; ++k)
       if (err[k]) std::rethrow_exception(err[k]);
   }
+  tr.mark(side == kTileSideAt ? "    plan A': tiles" : "    plan A: tiles");
   std::vector<Tile> tiles;
   std::vector<int32_t> cta_begin, cta_inst, inst_cta(K + 1), inst_split(K + 1);
   int32_t splits = 0, carries = 0;
@@ -315,6 +317,7 @@ void build_tile_plan(TilePlan<T>& plan, const DeviceMatrix& M, const std::vector
   }
   // the host vectors die at return: wait for the copies before they do
   CK(cudaStreamSynchronize(s));
+  tr.mark(side == kTileSideAt ? "    plan A': copies, interleave" : "    plan A: copies, interleave");
 }
 
 template void build_tile_plan<float>(TilePlan<float>&, const DeviceMatrix&, const std::vector<int32_t>&,
