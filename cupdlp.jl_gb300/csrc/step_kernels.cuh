@@ -329,7 +329,6 @@ __device__ __forceinline__ void step_decision(StepState& s, double f1, double f2
   s.total_iters += s.constant_step ? 0 : 1;
   s.kkt_passes += 1.0;
   s.attempts_in_chunk += 1;
-  const double omega = s.omega;
   const double tau = s.tau;
   const double inter = fabs(inter_signed);
   const double ndy = sqrt(dy2);
